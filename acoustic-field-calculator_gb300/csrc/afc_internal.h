@@ -1,0 +1,63 @@
+// Internal declarations shared by the CUDA kernels (.cu) and the C-ABI host layer (capi.cpp).
+// Nothing here is part of the public ABI; the public declarations live in include/*.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+
+namespace afc {
+
+// Tags of the reference C ABI (capi/src/type_inference_aux.rs:53-103).
+enum SourceType : int { SRC_SPHERE = 0, SRC_T4010A1 = 1 };
+enum FieldType : int { FIELD_PRESSURE = 0, FIELD_POWER = 1, FIELD_COMPLEX = 2 };
+enum CalcType : int { CALC_CPU = 0, CALC_ACCURATE = 1, CALC_GPU = 2 };
+enum AreaType : int { AREA_GRID1D = 0, AREA_GRID2D = 1, AREA_GRID3D = 2, AREA_SCATTER = 3 };
+// How the per-point sum over sources is accumulated.
+enum SumMode : int { SUM_PLAIN = 0, SUM_COMPENSATED = 1 };
+
+// Floats per source record in the reference ABI layout.
+inline int source_stride(int st) { return st == SRC_T4010A1 ? 9 : 6; }
+
+// One source as the field kernels read it (48 bytes, 16-byte aligned):
+//   a = (x, y, z, k)              position [mm], wavenumber [rad/mm]
+//   b = (nx, ny, nz, -alpha*log2e) direction, attenuation as a base-2 exponent per mm
+//   c = (amp, phase, 0, 0)        amplitude, phase [rad]
+struct __align__(16) PackedSource {
+    float4 a, b, c;
+};
+
+// A grid area: the point with index p = i0 + c0 * (i1 + c1 * i2) (first specified axis fastest,
+// observe_area/grid/grid_area.rs:105-229) has coordinate origin[ax_k] + (float)i_k * res along
+// axis ax_k, computed with one f32 multiply and one f32 add as the reference does.
+struct GridDev {
+    int64_t count[3];  // points along the 1st/2nd/3rd specified axis (1 for a fixed axis)
+    int axis[3];       // 0 = x, 1 = y, 2 = z, in specification order
+    float origin[3];   // x, y, z
+    float res;
+};
+
+// A set of observation points: a grid generated on the fly or explicit xyz triples.
+struct PointSet {
+    bool is_grid;
+    GridDev grid;
+    const float* pts;  // device, 3 floats per point (scatter)
+    int64_t m;
+};
+
+cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const float* atten,
+                                int64_t n, PackedSource* out, cudaStream_t s);
+
+cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
+                         const PointSet& ps, void* out, cudaStream_t s);
+
+// Kernels launched by this library since load (the bench reports the delta).
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+// Bytes written per point for a field type.
+inline size_t field_elem_bytes(int field) { return field == FIELD_COMPLEX ? 8 : 4; }
+
+}  // namespace afc

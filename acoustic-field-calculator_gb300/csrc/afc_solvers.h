@@ -1,0 +1,43 @@
+// Multi-focus phase solvers on the GPU: transfer matrix G, GS-PAT, GS and naive linear
+// synthesis (acoustic-field-optimizer/src/multiple_foci/).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+namespace afc {
+
+enum SolverKind : int { SOLVER_GSPAT = 0, SOLVER_GS = 1, SOLVER_NAIVE = 2 };
+
+// REPEAT of gs_pat.rs:17 and gs.rs:17.
+constexpr int kSolverRepeat = 100;
+// Largest focus count the single-block iteration kernels accept.
+constexpr int64_t kSolverMaxFoci = 4096;
+
+// Device workspace (bytes, 256-aligned pieces) for n sources and m foci.
+size_t solver_workspace_bytes(int64_t n, int64_t m);
+
+// Everything on the device: sources in the ABI layout (d_raw, stride 9 or 6 floats), d_k,
+// d_atten, foci (3 floats each), target amplitudes.  Writes (amp, phase) per source to d_out
+// (2n floats).  `ws` must hold solver_workspace_bytes(n, m) bytes, 256-byte aligned.
+cudaError_t launch_solver(int kind, int st, const float* d_raw, const float* d_k,
+                          const float* d_atten, int64_t n, const float* d_foci,
+                          const float* d_amps, int64_t m, int repeat, float* d_out, void* ws,
+                          cudaStream_t s);
+
+// Build the transfer matrix G (row-major m x n, float2) for the sources' current amplitudes
+// and zero phase into d_g; `ws_packed` holds 48 n bytes.
+cudaError_t launch_build_g(int st, const float* d_raw, const float* d_k, const float* d_atten,
+                           int64_t n, const float* d_foci, int64_t m, float2* d_g,
+                           void* ws_packed, cudaStream_t s);
+
+// Host-level: uploads, solves, and writes amp / phase into the host source array `src`
+// (ABI layout) in place.  Returns 0 on success, else fills *err.
+int solve_multi_focus(int kind, int st, float* src, const float* k, const float* atten,
+                      int64_t n, const float* foci, const float* amps, int64_t m,
+                      std::string* err);
+
+}  // namespace afc

@@ -1,0 +1,359 @@
+"""Benchmark of the direct source->point summation on the large-grid workload:
+3984 T4010A1 transducers (4 x 4 tiling of the 249-element array, random phases and amplitudes,
+attenuation 1.15e-2 /mm), complex pressure on a 256^3 grid at 0.5 mm (16,777,216 points),
+i.e. 6.68e10 source-point evaluations per step.  Metric: evaluations per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Arms
+  ours       `value`: the device-level C-ABI call (AFC_FieldGridDevice) with sources already
+             in HBM, timed with CUDA events on the launching stream; the L2 is flushed (a
+             256 MiB write) between timed steps, outside the events.
+             `e2e`: the reference-facing C-ABI call AFC_Calculate with host buffers: each step
+             uploads the sources and downloads the 134 MB complex field into the field
+             buffer (pinned host memory) -- wall-clock per call, the call synchronises.
+             `cpu_baseline`: the oracle (C restatement of the reference CPU calculator,
+             OpenMP over points) on a bounded z-slab of the same grid, on this host's cores.
+  reference  the reference's CPU calculator restated in C (the oracle: the Rust reference
+             cannot be built here), all host threads, each step one bounded z-slab sample.
+
+Multi-GPU (torchrun): replicas only -- every rank evaluates its own copy of the workload with
+no collective on the data path (weak scaling); `value` = evals of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "acoustic-field-calculator_gb300"))
+
+import workloads as W  # noqa: E402
+
+METRIC = "source-point evaluations/s (FP32 direct summation, complex field)"
+UNIT = "evals/s"
+# canonical per-evaluation cost of the summation (rsqrt, sqrt in acos, ex2, sin, cos on the
+# MUFU pipe; 32 FP32-pipe operations)
+MUFU_PER_EVAL = 5
+FP32_PER_EVAL = 32
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config_dict(w, extra=None):
+    d = {"workload": w.name, "sources": w.n, "grid": [256, 256, 256], "resolution_mm": 0.5,
+         "points": 256 ** 3, "evals_per_step": w.n * 256 ** 3, "field": "complex pressure",
+         "attenuation_per_mm": 1.15e-2, "seed": 1, "parallelism": "replicas (no collective)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ------------------------------------------------------------------ CPU (oracle) legs
+
+def cpu_slab(w, n_planes: int):
+    """The first n_planes z-planes of the grid as explicit points (the slab the CPU times)."""
+    lo, _ = w.grid.lo_hi()
+    i = np.arange(256, dtype=np.float32)
+    xs = lo[0] + i * np.float32(0.5)
+    ys = lo[1] + i * np.float32(0.5)
+    zs = lo[2] + np.arange(n_planes, dtype=np.float32) * np.float32(0.5)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1).astype(np.float32)
+
+
+def cpu_rate(w, pts, repeats=1):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O  # the CPU baseline only
+
+    O.field_f32(1, w.sources, w.k, w.atten, pts[:256], O.FIELD_COMPLEX)  # warm
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_COMPLEX)
+        times.append(time.perf_counter() - t0)
+    return times, O.max_threads()
+
+
+def cpu_baseline(w, target_s=12.0):
+    # calibrate on a quarter plane, then size the slab to ~target_s of CPU work
+    probe = cpu_slab(w, 1)[:16384]
+    t, threads = cpu_rate(w, probe)
+    per_pt = t[0] / len(probe)
+    planes = int(max(1, min(64, target_s / (per_pt * 65536))))
+    pts = cpu_slab(w, planes)
+    t, threads = cpu_rate(w, pts)
+    evals = len(pts) * w.n
+    return {"value": evals / t[0], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{planes} z-plane(s) of the 256^3 grid = {len(pts)} points x {w.n} "
+                      f"sources ({evals:.3e} evals) in {t[0]:.2f} s, oracle f32, "
+                      f"{threads} OpenMP threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = W.large_grid()
+    planes = 1
+    pts = cpu_slab(w, planes)
+    evals = len(pts) * w.n
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    for _ in range(max(0, args.warmup)):
+        O.field_f32(1, w.sources, w.k, w.atten, pts[:4096], O.FIELD_COMPLEX)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_COMPLEX)
+    dt = time.perf_counter() - t0
+    value = evals * args.steps / dt
+    threads = O.max_threads()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": config_dict(w, {"sample_points_per_step": len(pts)}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step: 1 z-plane of the grid ({len(pts)} points x "
+                                       f"{w.n} sources = {evals:.3e} evals); the reference is "
+                                       "Rust and cannot be built here, so its CPU calculator "
+                                       "runs as the C restatement in oracle/"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("nccl")
+    import afc
+
+    lib = afc.DLL
+    if lib.AFC_SetDevice(local) != 0:
+        raise RuntimeError(afc.last_error())
+    w = W.large_grid()
+    evals = w.n * 256 ** 3
+
+    # ---- device-resident arm (value)
+    system = afc.UniformSystem(300.0)
+    system.add_records(1, w.sources, w.k, w.atten)
+    area = afc.grid_from_spec(w.grid)
+    desc = area.grid_desc()
+    m = int(desc.count[0] * desc.count[1] * desc.count[2])
+    assert m == 256 ** 3
+    dev = torch.device("cuda", local)
+    d_src = torch.from_numpy(w.sources.reshape(-1)).to(dev)
+    d_k = torch.from_numpy(w.k).to(dev)
+    d_a = torch.from_numpy(w.atten).to(dev)
+    ws_bytes = lib.AFC_FieldWorkspaceBytes(w.n)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    out = torch.empty(2 * m, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def step():
+        rc = lib.AFC_FieldGridDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                     w.n, ctypes.byref(desc), out.data_ptr(), ws.data_ptr(),
+                                     ws_bytes, sh)
+        if rc != 0:
+            raise RuntimeError(afc.last_error())
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+
+    mufu = ctypes.c_double()
+    fp32 = ctypes.c_double()
+    clk = ctypes.c_double()
+    nsm = ctypes.c_int32()
+    lib.AFC_MeasureIssueRates(ctypes.byref(mufu), ctypes.byref(fp32), ctypes.byref(clk),
+                              ctypes.byref(nsm))
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        launches0 = lib.AFC_KernelLaunchCount()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)  # L2 flush, outside the timed events
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        launches = lib.AFC_KernelLaunchCount() - launches0
+        if dist:
+            dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) * 1e-3
+    if dist:
+        tt = torch.tensor([total_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_s = float(tt.item())
+    value = evals * args.steps * world / total_s
+    per_gpu = evals * args.steps / total_s
+
+    # ---- end-to-end arm through AFC_Calculate (host buffers)
+    calc = afc.GpuCalculator()
+    field = afc.ComplexPressureFieldBuffer()
+    for _ in range(2):
+        calc.calculate_raw(system, area, field)
+    e2e_steps = max(1, min(args.steps, 5))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        calc.calculate_raw(system, area, field)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist:
+        tt = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    h2d = w.n * (9 + 2) * 4
+    d2h = m * 8
+
+    # ---- roofline of the summation kernel (FP32 + MUFU issue)
+    clock_summary = clocks.summary()
+    sm_mhz = clock_summary.get("sm_mhz") or clk.value / 1e6
+    peak_measured = min(mufu.value / MUFU_PER_EVAL, fp32.value / FP32_PER_EVAL)
+    peak_nominal = nsm.value * sm_mhz * 1e6 * min(16 / MUFU_PER_EVAL, 128 / FP32_PER_EVAL)
+    roofline = {
+        "bound": "fp32+sfu issue (compute)",
+        "achieved": per_gpu, "unit": "evals/s",
+        "peak": peak_measured, "frac": per_gpu / peak_measured if peak_measured else None,
+        "peak_source": "measured here: MUFU and FFMA microbenchmarks (AFC_MeasureIssueRates), "
+                       f"peak = min(mufu/{MUFU_PER_EVAL}, fp32/{FP32_PER_EVAL})",
+        "mufu_ops_per_s": mufu.value, "fp32_ops_per_s": fp32.value,
+        "calibration_sm_clock_mhz": clk.value / 1e6,
+        "peak_nominal_at_sampled_clock": peak_nominal,
+        "frac_of_nominal": per_gpu / peak_nominal if peak_nominal else None,
+        "traffic": None,
+        "hbm_write_gbs": d2h / (total_s / args.steps) / 1e9,
+    }
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": config_dict(w, {"l2": "flushed between timed steps (256 MiB write)"}),
+            "e2e": {"value": evals * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                    "api": "AFC_Calculate (reference C ABI), host buffers"},
+            "gpu_launches": int(launches), "roofline": roofline, "clocks": clock_summary,
+            "wall_s_timed": wall}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+/*
+ * afc_gpu.h -- device-pointer entry points of libafccapi.so (all NEW: the reference ABI has
+ * no device-level calls).
+ *
+ * They run the same kernels as AFC_Calculate but take device buffers and a CUDA stream, so a
+ * caller that keeps sources, points and results resident in GPU memory pays no host<->device
+ * copies.  The work they replace is the reference's internal Vulkan dispatch
+ * (acoustic-field-calculator/src/gpu/field_buffer/pressure_field.rs:48-255 and the shader
+ * assets/shaders/cpressure_base.comp:43-71) and the CPU loop
+ * (calculator/cpu_calculator.rs:43-56).
+ *
+ * Conventions: pointers named d_* are device pointers on the current CUDA device; `stream` is
+ * a cudaStream_t (NULL = legacy default stream); calls are asynchronous with respect to the
+ * host and return 0 on success or a negative AFC_ERR_* code (AFC_GetLastError has the text).
+ * Source records use the AfcT4010A1 / AfcSphereWaveSource layouts of afccapi.h.
+ */
+#ifndef AFC_GPU_H
+#define AFC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    AFC_OK = 0,
+    AFC_ERR_INVALID = -1,   /* bad tag, size, pointer or alignment */
+    AFC_ERR_CUDA = -2,      /* a CUDA call failed */
+    AFC_ERR_NO_DEVICE = -3, /* no usable CUDA device */
+    AFC_ERR_TOO_LARGE = -4, /* a size exceeds a documented maximum */
+    AFC_ERR_UNSUPPORTED = -5
+};
+
+/* Accumulation of the per-point sum: plain FP32 in source order (the CPU / GPU calculators)
+ * or compensated (the Accurate calculator). */
+enum { AFC_SUM_PLAIN = 0, AFC_SUM_COMPENSATED = 1 };
+
+/* A grid observation area.  Point p = i0 + count[0] * (i1 + count[1] * i2) lies at
+ * origin[axis_k - 1] + (float)i_k * res along axis_k; the first specified axis varies fastest
+ * (observe_area/grid/grid_area.rs:105-229). */
+typedef struct AfcGridDesc {
+    uint64_t count[3]; /* points along the 1st, 2nd, 3rd specified axis (1 for a fixed axis) */
+    int32_t axis[3];   /* axis codes X = 1, Y = 2, Z = 3 in specification order */
+    float origin[3];   /* x, y, z of point 0 */
+    float res;         /* spacing [mm] */
+} AfcGridDesc;
+
+/* Describe a grid area handle (dimension 1, 2 or 3) for the device calls. */
+int32_t AFC_GridDescFromArea(void *grid_handle, int32_t dimension, AfcGridDesc *out);
+
+/* Bytes of device workspace the field calls need for n sources (16-byte aligned buffer). */
+size_t AFC_FieldWorkspaceBytes(uint64_t n_sources);
+
+/* Field of n sources on a grid.  d_out receives count[0]*count[1]*count[2] floats (pressure,
+ * power) or float2 (complex). */
+int32_t AFC_FieldGridDevice(int32_t source_type, int32_t field_type, int32_t sum_mode,
+                            const float *d_sources, const float *d_wavenums,
+                            const float *d_attens, uint64_t n, const AfcGridDesc *grid,
+                            void *d_out, void *d_workspace, size_t workspace_bytes,
+                            void *stream);
+
+/* Field of n sources on m explicit points (3 floats each). */
+int32_t AFC_FieldScatterDevice(int32_t source_type, int32_t field_type, int32_t sum_mode,
+                               const float *d_sources, const float *d_wavenums,
+                               const float *d_attens, uint64_t n, const float *d_points,
+                               uint64_t m, void *d_out, void *d_workspace,
+                               size_t workspace_bytes, void *stream);
+
+/* Measure, on the current device, the MUFU (special-function) and FP32 FMA result rates
+ * [operations/s] with dependency-free microbenchmarks, the SM clock [Hz] while they run, and
+ * the SM count.  These are the denominators of the direct summation's roofline. */
+int32_t AFC_MeasureIssueRates(double *mufu_per_s, double *fp32_per_s, double *sm_clock_hz,
+                              int32_t *sm_count);
+
+/* Select the device that calculators and solvers created afterwards on this thread use (the
+ * reference's Vulkan calculator always takes the first device, gpu/gpu_calculator.rs:34-37;
+ * the default here is also device 0).  The device-level calls follow their stream's device. */
+int32_t AFC_SetDevice(int32_t device);
+
+/* Number of CUDA devices visible to this library (0 when none or the driver is unusable). */
+int32_t AFC_CudaDeviceCount(void);
+
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t AFC_KernelLaunchCount(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AFC_GPU_H */

@@ -1,0 +1,317 @@
+"""Parity of the GPU field kernels with the oracle, through the reference-facing C ABI
+(AFC_Calculate, driven like the reference's python/afc/afc.py) and the device-level ABI.
+
+Tolerance (the stated bar): max |p_gpu - p_ref| over points <= 1e-4 * max |p_ref|, with
+p_ref the oracle's restatement of the reference CPU calculator (float32) and, where stated,
+its float64 twin.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def rel_err(p, ref):
+    p = np.asarray(p)
+    ref = np.asarray(ref)
+    return float(np.max(np.abs(p - ref)) / np.max(np.abs(ref)))
+
+
+def make_system(afc, st, records, k, atten):
+    s = afc.UniformSystem(300.0)
+    s.add_records(st, records, k, atten)
+    return s
+
+
+def random_sources(rng, st, n, spread=60.0, atten=0.005):
+    pos = rng.uniform(-spread, spread, (n, 3)).astype(np.float32)
+    pos[:, 2] = rng.uniform(-5, 5, n)
+    amp = rng.uniform(0.2, 1.0, n).astype(np.float32)
+    ph = rng.uniform(-np.pi, np.pi, n).astype(np.float32)
+    if st == 1:
+        rec = W.t4010a1_records(pos, amp, ph)
+        d = rng.normal(size=(n, 3)) * np.array([0.3, 0.3, 0.0]) + np.array([0, 0, 1.0])
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rec[:, 3:6] = d
+    else:
+        rec = W.sphere_records(pos, amp, ph)
+    k = rng.uniform(0.70, 0.75, n).astype(np.float32)
+    a = np.full(n, atten, np.float32)
+    return rec, k, a
+
+
+def random_points(rng, m):
+    pts = rng.uniform(-80, 80, (m, 3)).astype(np.float32)
+    pts[:, 2] = rng.uniform(30, 200, m)
+    return pts
+
+
+def scatter(afc, pts):
+    area = afc.ScatterArea()
+    area.add_observe_points(pts)
+    return area
+
+
+FIELDS = {0: "PressureFieldBuffer", 1: "PowerFieldBuffer", 2: "ComplexPressureFieldBuffer"}
+CALCS = ["CpuCalculator", "AccurateCalculator", "GpuCalculator"]
+
+
+def check_field(out, ref_c, field):
+    """Compare a field buffer with the oracle's complex field."""
+    if field == 2:
+        assert rel_err(out, ref_c) <= TOL
+    elif field == 0:
+        assert rel_err(out, np.abs(ref_c)) <= TOL
+    else:
+        assert rel_err(out, np.abs(ref_c) ** 2) <= 2 * TOL
+
+
+def test_single_focus_all_calculators(gpu):
+    afc = gpu
+    w = W.single_focus()
+    s = make_system(afc, 1, w.sources, w.k, w.atten)
+    area = afc.grid_from_spec(w.grid)
+    assert area.get_size() == (101, 101, 1)
+    lo, hi = w.grid.lo_hi()
+    pts = O.grid_points(2, lo, hi, w.grid.res, w.grid.axes)
+    ref = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_PRESSURE)
+    ref64 = np.abs(O.field_f64(1, w.sources, w.k, w.atten, pts))
+    for calc in CALCS:
+        out = getattr(afc, calc)().calculate(s, area, afc.PressureFieldBuffer())
+        assert out.shape == (101 * 101,)
+        e = rel_err(out, ref)
+        print(f"single focus {calc}: max err / peak vs f32 oracle {e:.2e}, "
+              f"vs f64 {rel_err(out, ref64):.2e}")
+        assert e <= TOL
+        assert rel_err(out, ref64) <= TOL
+    # the focus is the peak and sits at the grid centre (reference example)
+    assert np.argmax(ref) == 50 * 101 + 50
+
+
+@pytest.mark.parametrize("st", [0, 1])
+@pytest.mark.parametrize("field", [0, 1, 2])
+@pytest.mark.parametrize("calc", CALCS)
+def test_scatter_random(gpu, st, field, calc):
+    afc = gpu
+    rng = np.random.default_rng(100 + 10 * st + field)
+    rec, k, a = random_sources(rng, st, 37)
+    pts = random_points(rng, 1000)
+    s = make_system(afc, st, rec, k, a)
+    out = getattr(afc, calc)().calculate(s, scatter(afc, pts), getattr(afc, FIELDS[field])())
+    ref = O.field_f32(st, rec, k, a, pts, O.FIELD_COMPLEX)
+    check_field(out, ref, field)
+
+
+@pytest.mark.parametrize("dim,axes", [(1, (1, 2, 3)), (1, (3, 2, 1)), (2, (1, 2, 3)),
+                                      (2, (2, 1, 3)), (2, (3, 1, 2)), (3, (1, 2, 3)),
+                                      (3, (3, 1, 2)), (3, (2, 3, 1))])
+def test_grid_orders(gpu, dim, axes):
+    afc = gpu
+    rng = np.random.default_rng(7 + dim)
+    rec, k, a = random_sources(rng, 1, 50)
+    ranges = [(-20.0, 25.0), (-10.0, 30.0), (60.0, 95.0)]
+    res = 1.5 if dim == 3 else 0.7
+    spec_ranges = []
+    for j, ax in enumerate(axes):
+        lo_, hi_ = ranges[ax - 1]
+        spec_ranges.append((lo_, hi_) if j < dim else (lo_, lo_))
+    g = W.GridSpec(dim, spec_ranges, res, axes)
+    s = make_system(afc, 1, rec, k, a)
+    area = afc.grid_from_spec(g)
+    lo, hi = g.lo_hi()
+    pts = O.grid_points(dim, lo, hi, res, axes)
+    out = afc.GpuCalculator().calculate(s, area, afc.ComplexPressureFieldBuffer())
+    assert out.shape[0] == len(pts)
+    ref = O.field_f32(1, rec, k, a, pts)
+    assert rel_err(out, ref) <= TOL
+
+
+@pytest.mark.parametrize("n,m", [(1, 1), (1, 1025), (257, 1), (513, 1023), (256, 1024),
+                                 (1000, 3)])
+def test_tails(gpu, n, m):
+    afc = gpu
+    rng = np.random.default_rng(n * 7 + m)
+    rec, k, a = random_sources(rng, 1, n)
+    pts = random_points(rng, m)
+    s = make_system(afc, 1, rec, k, a)
+    out = afc.GpuCalculator().calculate(s, scatter(afc, pts), afc.ComplexPressureFieldBuffer())
+    ref = O.field_f32(1, rec, k, a, pts)
+    assert rel_err(out, ref) <= TOL
+
+
+def test_no_sources_gives_zero_field(gpu):
+    afc = gpu
+    # a native system with no sources (the Python wrapper creates it on the first add)
+    s2 = afc.UniformSystem(300.0)
+    s2.set_source_type(0)
+    afc.DLL.AFC_CreateUniformSystem(ctypes.byref(s2.handle), 300.0, 0)
+    area = afc.GridAreaBuilder().x_range((0, 10)).y_at(0).z_at(10).resolution(1).generate()
+    out = afc.GpuCalculator().calculate(s2, area, afc.PressureFieldBuffer())
+    assert out.shape == (11,) and np.all(out == 0)
+
+
+def test_empty_scatter_area(gpu):
+    afc = gpu
+    s = afc.UniformSystem(300.0)
+    s.add_wave_source(afc.SphereWaveSource((0, 0, 0), 1.0, 0.0, 40e3))
+    n, ptr = afc.GpuCalculator().calculate_raw(s, afc.ScatterArea(), afc.PressureFieldBuffer())
+    assert n == 0 and ptr
+
+
+def test_point_on_a_source_is_not_finite_like_the_reference(gpu):
+    afc = gpu
+    rec = W.sphere_records(np.array([[0, 0, 0], [5, 0, 0]], np.float32), 1.0, 0.0)
+    k = np.full(2, 0.7, np.float32)
+    a = np.zeros(2, np.float32)
+    pts = np.array([[0, 0, 0], [0, 0, 50]], np.float32)
+    s = make_system(afc, 0, rec, k, a)
+    out = afc.GpuCalculator().calculate(s, scatter(afc, pts), afc.ComplexPressureFieldBuffer())
+    ref = O.field_f32(0, rec, k, a, pts)
+    assert not np.isfinite(out[0]) and not np.isfinite(ref[0])
+    assert abs(out[1] - ref[1]) <= TOL * abs(ref[1])
+
+
+def test_in_place_source_mutation_is_seen(gpu):
+    """python/main.py:57-63 rewrites phases through AFC_GetWaveSources between calculations."""
+    afc = gpu
+    rng = np.random.default_rng(11)
+    rec, k, a = random_sources(rng, 1, 64)
+    pts = random_points(rng, 500)
+    s = make_system(afc, 1, rec, k, a)
+    area = scatter(afc, pts)
+    calc = afc.GpuCalculator()
+    f = afc.ComplexPressureFieldBuffer()
+    calc.calculate(s, area, f)
+    arr = s.get_wave_sources()
+    for i in range(len(arr)):
+        arr[i].phase = float(rng.uniform(-3, 3))
+        arr[i].amp = float(rng.uniform(0.1, 1))
+    out = calc.calculate(s, area, f)
+    ref = O.field_f32(1, s.records().copy(), k, a, pts)
+    assert rel_err(out, ref) <= TOL
+
+
+def test_scatter_points_added_between_calls(gpu):
+    afc = gpu
+    rng = np.random.default_rng(12)
+    rec, k, a = random_sources(rng, 0, 20)
+    pts = random_points(rng, 300)
+    s = make_system(afc, 0, rec, k, a)
+    area = scatter(afc, pts[:100])
+    calc = afc.CpuCalculator()
+    f = afc.PressureFieldBuffer()
+    first = calc.calculate(s, area, f).copy()
+    area.add_observe_points(pts[100:])
+    second = calc.calculate(s, area, f)
+    ref = np.abs(O.field_f32(0, rec, k, a, pts))
+    assert len(second) == 300
+    assert rel_err(second, ref) <= TOL
+    assert rel_err(first, ref[:100]) <= TOL
+
+
+def test_focal_point_then_field(gpu):
+    """Reference example flow: AFO_FocalPoint, then the pressure on an XY slice."""
+    afc = gpu
+    s = afc.UniformSystem(300.0)
+    pos = W.unit_array(10.18)
+    for p in pos:
+        s.add_wave_source(afc.T4010A1(tuple(p), (0, 0, 1), 1.0, 0.0, 40e3))
+    cen = W.array_center(pos)
+    afc.Optimizer.focus(s, (float(cen[0]), float(cen[1]), 150.0))
+    area = (afc.GridAreaBuilder().x_range((cen[0] - 50, cen[0] + 50))
+            .y_range((cen[1] - 50, cen[1] + 50)).z_at(150.0).resolution(1.0).generate())
+    out = afc.GpuCalculator().calculate(s, area, afc.PressureFieldBuffer())
+    k, a = O.wavenum_atten(300.0, 40e3)
+    n = len(pos)
+    lo = np.array([cen[0] - 50, cen[1] - 50, 150], np.float32)
+    hi = np.array([cen[0] + 50, cen[1] + 50, 150], np.float32)
+    pts = O.grid_points(2, lo, hi, 1.0, (1, 2, 3))
+    ref = O.field_f32(1, s.records().copy(), np.full(n, k, np.float32),
+                      np.full(n, a, np.float32), pts, O.FIELD_PRESSURE)
+    assert rel_err(out, ref) <= TOL
+
+
+def test_device_api_matches_c_abi(gpu):
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    rng = np.random.default_rng(13)
+    rec, k, a = random_sources(rng, 1, 300)
+    g = W.GridSpec(3, [(-20.0, 20.0), (-15.0, 15.0), (80.0, 100.0)], 1.0, (1, 2, 3))
+    s = make_system(afc, 1, rec, k, a)
+    area = afc.grid_from_spec(g)
+    host = afc.GpuCalculator().calculate(s, area, afc.ComplexPressureFieldBuffer())
+    desc = area.grid_desc()
+    m = int(desc.count[0] * desc.count[1] * desc.count[2])
+    d_src = torch.from_numpy(rec.reshape(-1)).cuda()
+    d_k = torch.from_numpy(k).cuda()
+    d_a = torch.from_numpy(a).cuda()
+    ws_bytes = afc.DLL.AFC_FieldWorkspaceBytes(len(k))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty(2 * m, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = afc.DLL.AFC_FieldGridDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                     len(k), ctypes.byref(desc), out.data_ptr(), ws.data_ptr(),
+                                     ws_bytes, stream)
+    assert rc == 0, afc.last_error()
+    torch.cuda.synchronize()
+    dev = out.cpu().numpy().view(np.complex64)
+    np.testing.assert_array_equal(dev, host.astype(np.complex64))
+    # the scatter entry point on the materialised grid gives the same numbers
+    lo, hi = g.lo_hi()
+    pts = torch.from_numpy(O.grid_points(3, lo, hi, 1.0, (1, 2, 3)).reshape(-1)).cuda()
+    out2 = torch.empty(2 * m, dtype=torch.float32, device="cuda")
+    rc = afc.DLL.AFC_FieldScatterDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(),
+                                        d_a.data_ptr(), len(k), pts.data_ptr(), m,
+                                        out2.data_ptr(), ws.data_ptr(), ws_bytes, stream)
+    assert rc == 0, afc.last_error()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out2.cpu().numpy().view(np.complex64), dev)
+
+
+def test_large_grid_subsample_vs_f64(gpu):
+    """The 3984-source, 256^3-point complex field, checked on a seeded 0.1 % subsample against
+    the float64 oracle (and the float32 oracle)."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    w = W.large_grid()
+    s = make_system(afc, 1, w.sources, w.k, w.atten)
+    area = afc.grid_from_spec(w.grid)
+    desc = area.grid_desc()
+    m = int(desc.count[0] * desc.count[1] * desc.count[2])
+    assert m == 256 ** 3
+    d_src = torch.from_numpy(w.sources.reshape(-1)).cuda()
+    d_k = torch.from_numpy(w.k).cuda()
+    d_a = torch.from_numpy(w.atten).cuda()
+    ws_bytes = afc.DLL.AFC_FieldWorkspaceBytes(w.n)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty(2 * m, dtype=torch.float32, device="cuda")
+    rc = afc.DLL.AFC_FieldGridDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                     w.n, ctypes.byref(desc), out.data_ptr(), ws.data_ptr(),
+                                     ws_bytes, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, afc.last_error()
+    torch.cuda.synchronize()
+    field = out.cpu().numpy().view(np.complex64)
+    rng = np.random.default_rng(2024)
+    idx = np.sort(rng.choice(m, m // 1000, replace=False))
+    lo, hi = w.grid.lo_hi()
+    i0 = idx % 256
+    i1 = (idx // 256) % 256
+    i2 = idx // 65536
+    pts = np.stack([lo[0] + i0.astype(np.float32) * np.float32(0.5),
+                    lo[1] + i1.astype(np.float32) * np.float32(0.5),
+                    lo[2] + i2.astype(np.float32) * np.float32(0.5)], axis=1).astype(np.float32)
+    ref64 = O.field_f64(1, w.sources, w.k, w.atten, pts)
+    ref32 = O.field_f32(1, w.sources, w.k, w.atten, pts)
+    e64 = rel_err(field[idx], ref64)
+    e32 = rel_err(field[idx], ref32)
+    rl2 = float(np.linalg.norm(field[idx] - ref64) / np.linalg.norm(ref64))
+    print(f"large grid subsample ({len(idx)} pts): max err/peak vs f64 {e64:.2e}, vs f32 oracle "
+          f"{e32:.2e}, oracle f32 vs f64 {rel_err(ref32, ref64):.2e}, rel-L2 vs f64 {rl2:.2e}")
+    assert e64 <= TOL and e32 <= TOL

@@ -1,0 +1,99 @@
+"""GPU GS-PAT / GS / naive (AFO_GSPAT, AFO_GS, AFO_Naive) against the float64 oracle
+restatement of acoustic-field-optimizer/src/multiple_foci/linear_synthesis/{gs_pat,gs,naive}.rs.
+
+The solvers write amp and phase into the system in place.  Compared quantity: the complex
+drive q_j = amp_j exp(i phase_j); bar: max |q_gpu - q_f64| <= tol * max |q_f64| with tol
+1e-3 (GS-PAT, 100 nonlinear FP32 iterations), 1e-5 (naive, one product) and 1e-2 (GS), and
+the field the drive produces at the foci."""
+import numpy as np
+import pytest
+
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(afc, w):
+    s = afc.UniformSystem(300.0)
+    s.add_records(1, w.sources, w.k, w.atten)
+    return s
+
+
+def _q(rec):
+    return rec[:, 6].astype(np.float64) * np.exp(1j * rec[:, 7].astype(np.float64))
+
+
+@pytest.mark.parametrize("m", [2, 8, 31, 64])
+def test_gspat_matches_f64(gpu, m):
+    afc = gpu
+    rng = np.random.default_rng(40 + m)
+    w, foci, amps = W.gspat_request(rng, m)
+    s = _system(afc, w)
+    afc.Optimizer.gs_pat(s, foci, amps)
+    got = s.records().copy()
+    ref_src, q_ref = O.gspat_f64(1, w.sources, w.k, w.atten, foci, amps)
+    e = np.max(np.abs(_q(got) - q_ref)) / np.max(np.abs(q_ref))
+    p_gpu = np.abs(O.field_f64(1, got, w.k, w.atten, foci))
+    p_ref = np.abs(O.field_f64(1, ref_src, w.k, w.atten, foci))
+    ef = np.max(np.abs(p_gpu - p_ref)) / np.max(p_ref)
+    print(f"GS-PAT m={m}: max |dq|/max|q| = {e:.2e}, focus amplitude err {ef:.2e}")
+    assert e <= 1e-3
+    assert ef <= 1e-3
+    # positions, directions and frequencies are untouched
+    np.testing.assert_array_equal(got[:, [0, 1, 2, 3, 4, 5, 8]], w.sources[:, [0, 1, 2, 3, 4, 5, 8]])
+
+
+def test_naive_matches_f64(gpu):
+    afc = gpu
+    rng = np.random.default_rng(77)
+    w, foci, amps = W.gspat_request(rng, 16)
+    s = _system(afc, w)
+    afc.Optimizer.naive(s, foci, amps)
+    got = s.records().copy()
+    _, q_ref = O.naive_f64(1, w.sources, w.k, w.atten, foci, amps)
+    e = np.max(np.abs(_q(got) - q_ref)) / np.max(np.abs(q_ref))
+    print(f"naive: {e:.2e}")
+    assert e <= 1e-5
+
+
+def test_gs_matches_f64(gpu):
+    afc = gpu
+    rng = np.random.default_rng(78)
+    w, foci, amps = W.gspat_request(rng, 8)
+    s = _system(afc, w)
+    afc.Optimizer.gs(s, foci, amps)
+    got = s.records().copy()
+    ref_src, q_ref = O.gs_f64(1, w.sources, w.k, w.atten, foci, amps)
+    e = np.max(np.abs(_q(got) - q_ref)) / np.max(np.abs(q_ref))
+    print(f"GS: {e:.2e}")
+    assert e <= 1e-2
+
+
+def test_gspat_then_field(gpu):
+    """Reference flow (examples/foci.rs:151-153): solve, then evaluate an XY slice."""
+    afc = gpu
+    rng = np.random.default_rng(79)
+    w, foci, amps = W.gspat_request(rng, 6)
+    s = _system(afc, w)
+    afc.Optimizer.gs_pat(s, foci, amps)
+    z = float(np.mean(foci[:, 2]))
+    cen = W.array_center(W.tiled_array(2, 2))
+    area = (afc.GridAreaBuilder().x_range((cen[0] - 100, cen[0] + 100))
+            .y_range((cen[1] - 100, cen[1] + 100)).z_at(z).resolution(1.0).generate())
+    assert area.get_size() == (201, 201, 1)
+    out = afc.GpuCalculator().calculate(s, area, afc.PressureFieldBuffer())
+    lo = np.array([cen[0] - 100, cen[1] - 100, z], np.float32)
+    hi = np.array([cen[0] + 100, cen[1] + 100, z], np.float32)
+    pts = O.grid_points(2, lo, hi, 1.0, (1, 2, 3))
+    ref = O.field_f32(1, s.records().copy(), w.k, w.atten, pts, O.FIELD_PRESSURE)
+    assert np.max(np.abs(out - ref)) <= 1e-4 * np.max(ref)
+
+
+def test_empty_focus_list(gpu):
+    afc = gpu
+    rng = np.random.default_rng(80)
+    w, _, _ = W.gspat_request(rng, 2, tiles=(1, 1))
+    s = _system(afc, w)
+    afc.Optimizer.gs_pat(s, np.zeros((0, 3), np.float32), np.zeros(0, np.float32))
+    assert np.all(s.records()[:, 6] == 0)
