@@ -161,6 +161,8 @@ class Calculator:
         return size, ptr
 
     def calculate(self, system, observe_area, field):
+        """Returns a numpy copy of the result (the reference returns a view of the field
+        buffer, which dangles once the buffer is freed or grown; a copy cannot)."""
         size, ptr = self.calculate_raw(system, observe_area, field)
         fptr = ctypes.cast(ptr, POINTER(c_float))
         if field.get_type() == 2:
@@ -170,7 +172,7 @@ class Calculator:
             return carray.view(np.complex64).reshape(size).astype(np.complex128)
         if size == 0:
             return np.zeros(0, np.float32)
-        return np.ctypeslib.as_array(fptr, shape=(size,))
+        return np.ctypeslib.as_array(fptr, shape=(size,)).copy()
 
     @staticmethod
     def get_type():

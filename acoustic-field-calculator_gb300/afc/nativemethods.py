@@ -111,7 +111,7 @@ NEW_EXPORTS = [
     "AFC_GetLastError", "AFC_ClearLastError",
     "AFC_GridDescFromArea", "AFC_FieldWorkspaceBytes", "AFC_FieldGridDevice",
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
-    "AFC_MeasureIssueRates", "AFC_SetDevice",
+    "AFC_MeasurePipeRates", "AFC_SetDevice",
 ]
 
 
@@ -235,8 +235,8 @@ def __init_new():
     AFC_DLL.AFC_KernelLaunchCount.restype = c_uint64
     AFC_DLL.AFC_CudaDeviceCount.argtypes = []
     AFC_DLL.AFC_CudaDeviceCount.restype = c_int32
-    AFC_DLL.AFC_MeasureIssueRates.argtypes = [POINTER(c_double), POINTER(c_double),
-                                              POINTER(c_double), POINTER(c_int32)]
-    AFC_DLL.AFC_MeasureIssueRates.restype = c_int32
+    AFC_DLL.AFC_MeasurePipeRates.argtypes = [POINTER(c_double), POINTER(c_double),
+                                             POINTER(c_int32)]
+    AFC_DLL.AFC_MeasurePipeRates.restype = c_int32
     AFC_DLL.AFC_SetDevice.argtypes = [c_int32]
     AFC_DLL.AFC_SetDevice.restype = c_int32

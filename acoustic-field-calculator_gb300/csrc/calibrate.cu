@@ -1,7 +1,9 @@
-// Issue-rate microbenchmarks that measure the roofline of the direct summation on the GPU it
-// runs on: MUFU (SFU) results per second, FP32 FMA results per second, and the SM clock seen
-// while they run.  The field kernel's per-pair cost is quoted in these units (5 MUFU + 32 FP32
-// operations per source-point evaluation), so evals/s peak = min(mufu/5, fp32/32).
+// Pipe-rate microbenchmarks that measure the roofline of the direct summation on the GPU it
+// runs on: results per second of each MUFU (special-function unit) operation the summation
+// uses (ex2, rsqrt, sqrt, sin, cos), FP32 FMA results per second, and the SM clock seen while
+// they run.  The summation's canonical per-evaluation cost is one of each of those MUFU
+// operations plus 32 FP32 operations, so evals/s peak = min(1 / sum_op(1 / rate_op),
+// fp32 / 32).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -16,18 +18,35 @@ constexpr int kChains = 8;
 constexpr int kIters = 2048;
 constexpr int kCalThreads = 256;
 
-// x <- 2^x - 1 keeps every chain in [-0.5, 0): one MUFU.EX2 and one FADD per step.
+// One MUFU operation per step on kChains independent chains.  Op 0: x <- 2^x - 1 (ex2, plus
+// one FADD), 1: x <- rsqrt(x), 2: x <- sqrt(x), 3: x <- sin(x), 4: x <- cos(x); every chain
+// stays bounded.
+template <int OP>
+__device__ __forceinline__ float mufu_step(float x) {
+    float y;
+    if constexpr (OP == 0) {
+        asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        y -= 1.0f;
+    } else if constexpr (OP == 1) {
+        asm volatile("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    } else if constexpr (OP == 2) {
+        asm volatile("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    } else if constexpr (OP == 3) {
+        asm volatile("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    } else {
+        asm volatile("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    }
+    return y;
+}
+
+template <int OP>
 __global__ void __launch_bounds__(kCalThreads) mufu_rate_kernel(float* sink, float seed) {
     float x[kChains];
 #pragma unroll
-    for (int c = 0; c < kChains; ++c) x[c] = -0.25f - 0.01f * c - seed * threadIdx.x;
+    for (int c = 0; c < kChains; ++c) x[c] = (OP == 0 ? -0.25f : 0.75f) - 0.01f * c - seed * threadIdx.x;
     for (int i = 0; i < kIters; ++i) {
 #pragma unroll
-        for (int c = 0; c < kChains; ++c) {
-            float y;
-            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
-            x[c] = y - 1.0f;
-        }
+        for (int c = 0; c < kChains; ++c) x[c] = mufu_step<OP>(x[c]);
     }
     float s = 0.f;
 #pragma unroll
@@ -68,8 +87,30 @@ __global__ void clock_kernel(unsigned long long* out, unsigned long long spin_ns
 }  // namespace
 }  // namespace afc
 
-extern "C" int32_t AFC_MeasureIssueRates(double* mufu_per_s, double* fp32_per_s,
-                                         double* sm_clock_hz, int32_t* sm_count) {
+namespace afc {
+namespace {
+
+template <int OP>
+double time_mufu(int blocks, float* sink, cudaEvent_t e0, cudaEvent_t e1, double ops) {
+    double best = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+        float ms = 0.f;
+        cudaEventRecord(e0);
+        mufu_rate_kernel<OP><<<blocks, kCalThreads>>>(sink, 1e-7f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        count_launch();
+        if (rep > 0 && ms > 0) best = fmax(best, ops / (ms * 1e-3));
+    }
+    return best;
+}
+
+}  // namespace
+}  // namespace afc
+
+// rates[0..4] = ex2, rsqrt, sqrt, sin, cos results/s; rates[5] = FP32 FMA results/s.
+extern "C" int32_t AFC_MeasurePipeRates(double* rates, double* sm_clock_hz, int32_t* sm_count) {
     using namespace afc;
     int dev = 0;
     cudaDeviceProp prop;
@@ -88,23 +129,23 @@ extern "C" int32_t AFC_MeasureIssueRates(double* mufu_per_s, double* fp32_per_s,
     cudaEventCreate(&e1);
     const int blocks = prop.multiProcessorCount * 8;
     const double ops = static_cast<double>(blocks) * kCalThreads * kChains * kIters;
-    float ms = 0.f;
-    double best_mufu = 0, best_ffma = 0;
-    for (int rep = 0; rep < 4; ++rep) {
-        cudaEventRecord(e0);
-        mufu_rate_kernel<<<blocks, kCalThreads>>>(sink, 1e-7f);
-        cudaEventRecord(e1);
-        cudaEventSynchronize(e1);
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep > 0 && ms > 0) best_mufu = fmax(best_mufu, ops / (ms * 1e-3));
+    rates[0] = time_mufu<0>(blocks, sink, e0, e1, ops);
+    rates[1] = time_mufu<1>(blocks, sink, e0, e1, ops);
+    rates[2] = time_mufu<2>(blocks, sink, e0, e1, ops);
+    rates[3] = time_mufu<3>(blocks, sink, e0, e1, ops);
+    rates[4] = time_mufu<4>(blocks, sink, e0, e1, ops);
+    double best_ffma = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+        float ms = 0.f;
         cudaEventRecord(e0);
         ffma_rate_kernel<<<blocks, kCalThreads>>>(sink, 1e-7f);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
         cudaEventElapsedTime(&ms, e0, e1);
+        count_launch();
         if (rep > 0 && ms > 0) best_ffma = fmax(best_ffma, ops / (ms * 1e-3));
-        count_launch(2);
     }
+    rates[5] = best_ffma;
     clock_kernel<<<1, 1>>>(clk, 20000000ull);
     count_launch();
     unsigned long long h[2] = {0, 0};
@@ -114,8 +155,6 @@ extern "C" int32_t AFC_MeasureIssueRates(double* mufu_per_s, double* fp32_per_s,
     cudaFree(sink);
     cudaFree(clk);
     if (e != cudaSuccess) return AFC_ERR_CUDA;
-    if (mufu_per_s) *mufu_per_s = best_mufu;
-    if (fp32_per_s) *fp32_per_s = best_ffma;
     if (sm_clock_hz) *sm_clock_hz = h[1] ? static_cast<double>(h[0]) / (h[1] * 1e-9) : 0.0;
     return AFC_OK;
 }

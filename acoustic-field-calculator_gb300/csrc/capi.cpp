@@ -159,7 +159,7 @@ struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
     cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
+        if (p && bytes <= cap) return cudaSuccess;
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
@@ -179,7 +179,7 @@ struct PinnedBuf {
     void* p = nullptr;
     size_t cap = 0;
     cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
+        if (p && bytes <= cap) return cudaSuccess;
         if (p) cudaFreeHost(p);
         p = nullptr;
         cap = 0;

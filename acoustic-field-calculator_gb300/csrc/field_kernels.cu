@@ -7,17 +7,18 @@
 // apply the field transform of field_buffer/{pressure,power,complex_pressure}_field.rs:35-37.
 //
 // Layout and schedule
-//   * Sources are packed once per call (PackedSource, 48 B) and streamed through shared memory
-//     in tiles of kTile; every thread of a block reads the same source at the same time, so the
-//     shared-memory reads are broadcasts.
-//   * Each thread owns kPPT observation points spaced kThreads apart, so each of its kPPT
-//     stores is part of one contiguous, coalesced warp store (4 B or 8 B per point).
+//   * Sources are packed once per call (PackedSource, 48 B) and staged tile by tile into
+//     shared memory with every per-source scalar stored twice ((v, v) pairs), so that one
+//     LDS.128 yields two packed f32x2 broadcast operands.  All threads of a block read the
+//     same source at the same time: shared-memory broadcasts.
+//   * Each thread owns 2*PAIRS observation points spaced kThreads apart and processes them two
+//     at a time with the sm_100 packed FP32 instructions (FFMA2 / FMUL2 / FADD2), which halves
+//     the FP32 instructions issued; MUFU operations stay per point.  The PAIRS pairs of one
+//     source are independent, so their instructions interleave; the rare pairs whose theta
+//     lies next to a directivity bin edge are collected in a bit mask and corrected after the
+//     source, off the interleaved path.
+//   * Each of the 2*PAIRS stores is one contiguous, coalesced warp store (4 B or 8 B a point).
 //   * Grid points are generated from the grid description, never read from memory.
-//
-// Per pair: 3 sub, r^2, rsqrt (MUFU), cos(theta), acos, the directivity cubic (coefficients
-// from a shared-memory table indexed by the 10-degree bin), ex2 (MUFU) for the attenuation,
-// phase = phi + k r reduced to [-pi, pi] by a two-constant Cody-Waite step, then __sincosf
-// (MUFU sin + cos) and two FMAs into the accumulators.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,13 +30,20 @@ namespace afc {
 
 namespace {
 
+using namespace dev;
+
 constexpr int kThreads = 256;  // threads per block
-constexpr int kPPT = 4;        // observation points per thread
 constexpr int kTile = 256;     // sources per shared-memory tile
 
-using dev::kLog2e;
+__constant__ float4 c_dir_table[kDirTableSize] = AFC_DIR_TABLE_INIT;
 
-__constant__ float4 c_dir_table[dev::kDirTableSize] = AFC_DIR_TABLE_INIT;
+// Shared-memory image of one source: five float4 of duplicated scalars.
+//   v0 = (-x, -x, -y, -y)   v1 = (-z, -z, k, k)   v2 = (nx, nx, ny, ny)
+//   v3 = (nz, nz, a2, a2)   v4 = (amp, amp, phase, phase)       a2 = -alpha * log2(e)
+struct SmemTile {
+    float4 v0[kTile], v1[kTile], v2[kTile], v3[kTile], v4[kTile];
+    float4 dir[kDirTableSize];
+};
 
 // Neumaier's compensated addition: sum + v with the lost low-order part added to comp.
 __device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
@@ -55,10 +63,7 @@ __device__ __forceinline__ void grid_point(const GridDev& g, int64_t p, float& x
     const int64_t q = p / g.count[0];
     const int64_t i1 = q % g.count[1];
     const int64_t i2 = q / g.count[1];
-    float v[3];
-    v[0] = g.origin[0];
-    v[1] = g.origin[1];
-    v[2] = g.origin[2];
+    float v[3] = {g.origin[0], g.origin[1], g.origin[2]};
     const int64_t idx[3] = {i0, i1, i2};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -76,35 +81,79 @@ __device__ __forceinline__ void grid_point(const GridDev& g, int64_t p, float& x
     z = v[2];
 }
 
-template <int ST, int FT, int SUM, bool GRID>
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+__device__ __forceinline__ float& lane_of(float2& v, int hi) { return hi ? v.y : v.x; }
+
+// Reduced phase phi + k r - n 2pi in [-pi, pi] for two points.
+__device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase) {
+    const float2 ph = fma2(k, r, phase);
+    const float2 nq = add2(fma2(ph, f2(kInv2Pi), f2(kRoundMagic)), f2(-kRoundMagic));
+    return fma2(nq, f2(-kTwoPiLo), fma2(nq, f2(-kTwoPiHi), ph));
+}
+
+// Correction for one point whose fast theta fell next to a bin edge: recompute the pair with
+// the same fast operations, then add w0 (D_exact - D_fast) (cos, sin) to the accumulators.
+template <int SUM>
+__device__ __noinline__ void edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
+                                             float4 v2, float4 v3, float4 v4, float px, float py,
+                                             float pz, float& re, float& im, float& cre,
+                                             float& cim) {
+    const float dx = px + v0.x, dy = py + v0.z, dz = pz + v1.x;
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float rinv = mufu_rsqrt(r2);
+    const float r = r2 * rinv;
+    const float w0 = (v4.x * rinv) * mufu_ex2(v3.z * r);
+    const float ct = fmaf(v3.x, dz, fmaf(v2.z, dy, v2.x * dx)) * rinv;
+    unsigned near;
+    const float d_fast = directivity2_fast(tab, make_float2(ct, ct), near).x;
+    const float d_exact = directivity_exact(tab, dx, dy, dz, v2.x, v2.z, v3.x);
+    const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
+    const float corr = w0 * (d_exact - d_fast);
+    if constexpr (SUM == SUM_PLAIN) {
+        re = fmaf(corr, mufu_cos(red), re);
+        im = fmaf(corr, mufu_sin(red), im);
+    } else {
+        neumaier_add(re, cre, corr * mufu_cos(red));
+        neumaier_add(im, cim, corr * mufu_sin(red));
+    }
+}
+
+template <int ST, int SUM, bool GRID, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
     field_direct_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
-                        const float* __restrict__ pts, int64_t m, void* __restrict__ out) {
-    __shared__ float4 s_a[kTile];
-    __shared__ float4 s_b[kTile];
-    __shared__ float2 s_c[kTile];
-    __shared__ float4 s_dir[dev::kDirTableSize];
-
-    if (threadIdx.x < dev::kDirTableSize) s_dir[threadIdx.x] = c_dir_table[threadIdx.x];
+                        const float* __restrict__ pts, int64_t m, int field,
+                        void* __restrict__ out) {
+    constexpr int kPPT = 2 * PAIRS;
+    __shared__ SmemTile sm;
+    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
 
     const int64_t base = static_cast<int64_t>(blockIdx.x) * (kThreads * kPPT) + threadIdx.x;
-    float px[kPPT], py[kPPT], pz[kPPT];
-    float re[kPPT], im[kPPT], cre[kPPT], cim[kPPT];
+    float2 PX[PAIRS], PY[PAIRS], PZ[PAIRS];
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         int64_t p = base + static_cast<int64_t>(k) * kThreads;
         if (p >= m) p = m - 1;  // computed but never stored
+        float x, y, z;
         if constexpr (GRID) {
-            grid_point(g, p, px[k], py[k], pz[k]);
+            grid_point(g, p, x, y, z);
         } else {
-            px[k] = __ldg(pts + 3 * p);
-            py[k] = __ldg(pts + 3 * p + 1);
-            pz[k] = __ldg(pts + 3 * p + 2);
+            x = __ldg(pts + 3 * p);
+            y = __ldg(pts + 3 * p + 1);
+            z = __ldg(pts + 3 * p + 2);
         }
-        re[k] = 0.f;
-        im[k] = 0.f;
-        cre[k] = 0.f;
-        cim[k] = 0.f;
+        lane_of(PX[k >> 1], k & 1) = x;
+        lane_of(PY[k >> 1], k & 1) = y;
+        lane_of(PZ[k >> 1], k & 1) = z;
+    }
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        RE[q] = f2(0.f);
+        IM[q] = f2(0.f);
+        CRE[q] = f2(0.f);
+        CIM[q] = f2(0.f);
     }
 
     for (int64_t t0 = 0; t0 < n; t0 += kTile) {
@@ -112,28 +161,63 @@ __global__ void __launch_bounds__(kThreads, 2)
         __syncthreads();
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
             const PackedSource s = src[t0 + j];
-            s_a[j] = s.a;
-            s_b[j] = s.b;
-            s_c[j] = make_float2(s.c.x, s.c.y);
+            sm.v0[j] = make_float4(-s.a.x, -s.a.x, -s.a.y, -s.a.y);
+            sm.v1[j] = make_float4(-s.a.z, -s.a.z, s.a.w, s.a.w);
+            sm.v2[j] = make_float4(s.b.x, s.b.x, s.b.y, s.b.y);
+            sm.v3[j] = make_float4(s.b.z, s.b.z, s.b.w, s.b.w);
+            sm.v4[j] = make_float4(s.c.x, s.c.x, s.c.y, s.c.y);
         }
         __syncthreads();
-#pragma unroll 2
+#pragma unroll 1
         for (int j = 0; j < cnt; ++j) {
-            const float4 a = s_a[j];
-            const float4 b = s_b[j];
-            const float2 c = s_c[j];
+            const float4 v0 = sm.v0[j], v1 = sm.v1[j], v3 = sm.v3[j], v4 = sm.v4[j];
+            float4 v2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (ST == SRC_T4010A1) v2 = sm.v2[j];
+            unsigned near_mask = 0;
 #pragma unroll
-            for (int k = 0; k < kPPT; ++k) {
-                float w, red;
-                dev::pair_terms<ST>(a, b, c.x, c.y, s_dir, px[k], py[k], pz[k], w, red);
-                float sn, cs;
-                __sincosf(red, &sn, &cs);
+            for (int q = 0; q < PAIRS; ++q) {
+                const float2 dx = add2(PX[q], lo2(v0));
+                const float2 dy = add2(PY[q], hi2(v0));
+                const float2 dz = add2(PZ[q], lo2(v1));
+                const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                const float2 rinv = make_float2(mufu_rsqrt(r2.x), mufu_rsqrt(r2.y));
+                const float2 r = mul2(r2, rinv);
+                const float2 ea = mul2(hi2(v3), r);
+                float2 w = mul2(mul2(lo2(v4), rinv),
+                                make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
+                if constexpr (ST == SRC_T4010A1) {
+                    const float2 ct =
+                        mul2(fma2(lo2(v3), dz, fma2(hi2(v2), dy, mul2(lo2(v2), dx))), rinv);
+                    unsigned near;
+                    w = mul2(w, directivity2_fast(sm.dir, ct, near));
+                    near_mask |= near << (2 * q);
+                }
+                const float2 red = reduce_phase2(hi2(v1), r, hi2(v4));
+                const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
+                const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
                 if constexpr (SUM == SUM_PLAIN) {
-                    re[k] = fmaf(w, cs, re[k]);
-                    im[k] = fmaf(w, sn, im[k]);
+                    RE[q] = fma2(w, cs, RE[q]);
+                    IM[q] = fma2(w, sn, IM[q]);
                 } else {
-                    neumaier_add(re[k], cre[k], w * cs);
-                    neumaier_add(im[k], cim[k], w * sn);
+                    const float2 tr = mul2(w, cs), ti = mul2(w, sn);
+                    neumaier_add(RE[q].x, CRE[q].x, tr.x);
+                    neumaier_add(RE[q].y, CRE[q].y, tr.y);
+                    neumaier_add(IM[q].x, CIM[q].x, ti.x);
+                    neumaier_add(IM[q].y, CIM[q].y, ti.y);
+                }
+            }
+            if constexpr (ST == SRC_T4010A1) {
+                if (near_mask) {
+#pragma unroll
+                    for (int k = 0; k < kPPT; ++k) {
+                        if (near_mask & (1u << k)) {
+                            const int q = k >> 1, h = k & 1;
+                            edge_correction<SUM>(sm.dir, v0, v1, v2, v3, v4, lane_of(PX[q], h),
+                                                 lane_of(PY[q], h), lane_of(PZ[q], h),
+                                                 lane_of(RE[q], h), lane_of(IM[q], h),
+                                                 lane_of(CRE[q], h), lane_of(CIM[q], h));
+                        }
+                    }
                 }
             }
         }
@@ -143,17 +227,18 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int k = 0; k < kPPT; ++k) {
         const int64_t p = base + static_cast<int64_t>(k) * kThreads;
         if (p >= m) break;
-        float vr = re[k], vi = im[k];
+        float vr = lane_of(RE[k >> 1], k & 1);
+        float vi = lane_of(IM[k >> 1], k & 1);
         if constexpr (SUM == SUM_COMPENSATED) {
-            vr = __fadd_rn(vr, cre[k]);
-            vi = __fadd_rn(vi, cim[k]);
+            vr = __fadd_rn(vr, lane_of(CRE[k >> 1], k & 1));
+            vi = __fadd_rn(vi, lane_of(CIM[k >> 1], k & 1));
         }
-        if constexpr (FT == FIELD_COMPLEX) {
+        if (field == FIELD_COMPLEX) {
             reinterpret_cast<float2*>(out)[p] = make_float2(vr, vi);
         } else {
             // norm_sqr = re*re + im*im without contraction (pressure_field.rs:35-37)
             const float ns = __fadd_rn(__fmul_rn(vr, vr), __fmul_rn(vi, vi));
-            reinterpret_cast<float*>(out)[p] = (FT == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
+            reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
         }
     }
 }
@@ -178,39 +263,48 @@ __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
     out[j] = p;
 }
 
-template <int ST, int FT, int SUM>
-cudaError_t launch_typed(const PackedSource* src, int64_t n, const PointSet& ps, void* out,
-                         cudaStream_t s) {
-    const int64_t per_block = static_cast<int64_t>(kThreads) * kPPT;
+int g_num_sms = 0;
+
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            g_num_sms = v;
+        else
+            return 148;
+    }
+    return g_num_sms;
+}
+
+template <int ST, int SUM, int PAIRS>
+cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
+                         void* out, cudaStream_t s) {
+    const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t blocks = (ps.m + per_block - 1) / per_block;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     if (ps.is_grid) {
-        field_direct_kernel<ST, FT, SUM, true>
-            <<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(src, n, ps.grid, nullptr, ps.m, out);
+        field_direct_kernel<ST, SUM, true, PAIRS><<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(
+            src, n, ps.grid, nullptr, ps.m, field, out);
     } else {
-        field_direct_kernel<ST, FT, SUM, false>
-            <<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(src, n, ps.grid, ps.pts, ps.m, out);
+        field_direct_kernel<ST, SUM, false, PAIRS><<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(
+            src, n, ps.grid, ps.pts, ps.m, field, out);
     }
     count_launch();
     return cudaGetLastError();
 }
 
-template <int ST, int FT>
-cudaError_t launch_sum(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
-                       void* out, cudaStream_t s) {
-    return sum_mode == SUM_COMPENSATED ? launch_typed<ST, FT, SUM_COMPENSATED>(src, n, ps, out, s)
-                                       : launch_typed<ST, FT, SUM_PLAIN>(src, n, ps, out, s);
-}
-
+// Points per thread: the most that still gives every SM two blocks (more points per thread
+// amortise the shared-memory reads; too few blocks leave SMs idle).
 template <int ST>
-cudaError_t launch_field_t(int field, int sum_mode, const PackedSource* src, int64_t n,
-                           const PointSet& ps, void* out, cudaStream_t s) {
-    switch (field) {
-        case FIELD_PRESSURE: return launch_sum<ST, FIELD_PRESSURE>(sum_mode, src, n, ps, out, s);
-        case FIELD_POWER: return launch_sum<ST, FIELD_POWER>(sum_mode, src, n, ps, out, s);
-        case FIELD_COMPLEX: return launch_sum<ST, FIELD_COMPLEX>(sum_mode, src, n, ps, out, s);
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
+                      int field, void* out, cudaStream_t s) {
+    if (sum_mode == SUM_COMPENSATED)
+        return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s);
+    const int64_t want = 2LL * num_sms();
+    if (ps.m >= want * kThreads * 8) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s);
+    if (ps.m >= want * kThreads * 4) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s);
+    return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s);
 }
 
 }  // namespace
@@ -230,8 +324,9 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
                          const PointSet& ps, void* out, cudaStream_t s) {
     if (ps.m <= 0) return cudaSuccess;
-    if (st == SRC_T4010A1) return launch_field_t<SRC_T4010A1>(field, sum_mode, src, n, ps, out, s);
-    if (st == SRC_SPHERE) return launch_field_t<SRC_SPHERE>(field, sum_mode, src, n, ps, out, s);
+    if (field < FIELD_PRESSURE || field > FIELD_COMPLEX) return cudaErrorInvalidValue;
+    if (st == SRC_T4010A1) return launch_st<SRC_T4010A1>(sum_mode, src, n, ps, field, out, s);
+    if (st == SRC_SPHERE) return launch_st<SRC_SPHERE>(sum_mode, src, n, ps, field, out, s);
     return cudaErrorInvalidValue;
 }
 

@@ -5,6 +5,17 @@
 //     d = x - s_j, r = |d|, theta = acos(n_j . d / r), D = directivity(theta)
 //     w = A_j D exp(-alpha_j r) / r,   phase = phi_j + k_j r
 // and the contribution w * (cos phase, sin phase).
+//
+// Fast path (every pair): rsqrt / ex2 / sqrt / sin / cos on the MUFU pipe (PTX .approx.ftz),
+// theta from an own-fit polynomial, everything else in FP32, two points at a time with the
+// sm_100 packed f32x2 instructions where both points take the same operation.
+//
+// The T4010A1 directivity is piecewise in 10-degree bins and jumps at 30, 40, 60 and 90
+// degrees (by 0.016, 0.003, 0.047 and 0.164).  A theta within rounding of a bin edge can land
+// in a different bin than the reference's f32 arithmetic puts it, which changes that pair's
+// term by up to 16 %.  Pairs whose fast theta lies within kEdgeMargin of an edge therefore take
+// directivity_exact(), which repeats the reference's f32 operations (no FMA, IEEE sqrt and
+// division, acos correctly rounded from double) so that the bin is the reference's.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,9 +32,32 @@ constexpr float kInv2Pi = 0.15915494309189535f;
 // remainder.
 constexpr float kTwoPiHi = 6.28318548202514648f;     // float(2*pi)
 constexpr float kTwoPiLo = -1.7484555314695172e-7f;  // 2*pi - float(2*pi)
+// (u + 1.5 * 2^23) - 1.5 * 2^23 rounds |u| < 2^22 to the nearest integer with two FADDs.
+constexpr float kRoundMagic = 12582912.0f;
+// 2^23: for 0 <= q < 2^23, q + 2^23 rounded upward is 2^23 + ceil(q), whose bit pattern minus
+// that of 2^23 (0x4B000000) is ceil(q) as an integer.
+constexpr float kTwo23 = 8388608.0f;
+constexpr int kTwo23Bits = 0x4B000000;
 // 10-degree directivity bins: ANGLE_DIV = PI / 18 (t4010a1.rs:71) and its reciprocal.
 constexpr float kAngleDiv = 3.14159265358979323846f / 18.0f;
 constexpr float kInvAngleDiv = 18.0f / 3.14159265358979323846f;
+// A fast theta closer than this to a bin edge [rad] takes the exact path.  The fast theta is
+// within ~1e-6 rad of the reference's (rsqrt and FMA rounding in cos(theta), 4e-7 from the
+// polynomial), so 1e-5 leaves a factor of ten.
+constexpr float kEdgeMargin = 1.0e-5f;
+constexpr float kEdgeBound = 0.5f * kAngleDiv - kEdgeMargin;
+// cos(theta) is clamped below at -0.03 (theta ~ 91.7 deg, directivity 0 beyond 90 deg).
+constexpr float kCosFloor = -0.03f;
+
+// acos(c) = sqrt(1 - c) * Q(c); Q fitted in fit_acos.py (float32 error <= 4e-7 rad on
+// [-0.03, 1]).
+constexpr float kAcos0 = 1.5707964897155762f;
+constexpr float kAcos1 = -0.21459674835205078f;
+constexpr float kAcos2 = 0.08885793387889862f;
+constexpr float kAcos3 = -0.04917646571993828f;
+constexpr float kAcos4 = 0.027550870552659035f;
+constexpr float kAcos5 = -0.011683782562613487f;
+constexpr float kAcos6 = 0.0024654590524733067f;
 
 // T4010A1 directivity coefficients (t4010a1.rs:18-69) as (a, b, c, d) per bin.  Entry 0
 // (theta == 0) evaluates to 1 like the reference's `0 => 1.0` arm, entries 1 and 2 are the
@@ -42,17 +76,118 @@ constexpr float kInvAngleDiv = 18.0f / 3.14159265358979323846f;
     }
 constexpr int kDirTableSize = 11;
 
-// T4010A1::directivity (t4010a1.rs:107-120): bin i = ceil(theta / ANGLE_DIV),
-// x = theta - (i - 1) * ANGLE_DIV, D = a + (b + (c + d x) x) x.  `tab` is the table above,
-// normally staged in shared memory.
-__device__ __forceinline__ float directivity(const float4* __restrict__ tab, float theta) {
-    const float fi = ceilf(theta * kInvAngleDiv);
-    int i = static_cast<int>(fi);  // NaN converts to 0, i.e. D = 1 as in the reference
-    i = min(i, 10);
+// ------------------------------------------------------------------ MUFU operations
+
+__device__ __forceinline__ float mufu_rsqrt(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float mufu_sqrt(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float mufu_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float mufu_sin(float x) {
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float mufu_cos(float x) {
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// ------------------------------------------------------------------ packed f32x2 helpers
+
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// ------------------------------------------------------------------ directivity
+
+// The reference's own f32 arithmetic for theta and its bin (uniform_medium.rs:113-116,
+// t4010a1.rs:107-120): |d| = sqrt((dx dx + dy dy) + dz dz), cos = ((nx dx + ny dy) + nz dz) / |d|,
+// theta = acos(cos) rounded to f32, i = ceil(theta / ANGLE_DIV).
+static __device__ __noinline__ float directivity_exact(const float4* __restrict__ tab, float dx,
+                                                float dy, float dz, float nx, float ny, float nz) {
+    const float dist = __fsqrt_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(nx, dx), __fmul_rn(ny, dy)), __fmul_rn(nz, dz));
+    const float ct = __fdiv_rn(dot, dist);
+    const float theta = __double2float_rn(acos(static_cast<double>(ct)));
+    const float q = ceilf(__fdiv_rn(theta, kAngleDiv));
+    if (!(q > 0.0f)) return 1.0f;  // bin 0, and NaN (`as usize` gives 0)
+    if (q > 9.0f) return 0.0f;
+    const int i = static_cast<int>(q);
     const float4 c = tab[i];
-    const float x = fmaf(-(fi - 1.0f), kAngleDiv, theta);
+    const float x = __fsub_rn(theta, __fmul_rn(__fsub_rn(static_cast<float>(i), 1.0f), kAngleDiv));
+    return __fadd_rn(c.x, __fmul_rn(__fadd_rn(c.y, __fmul_rn(__fadd_rn(c.z, __fmul_rn(c.w, x)), x)), x));
+}
+
+// Fast theta from cos(theta) for two points.
+__device__ __forceinline__ float2 acos2_fast(float2 ct) {
+    const float2 c = make_float2(fmaxf(ct.x, kCosFloor), fmaxf(ct.y, kCosFloor));
+    float2 om = fma2(c, f2(-1.0f), f2(1.0f));  // 1 - c
+    om.x = fmaxf(om.x, 0.0f);                  // c rounded above 1 -> theta 0
+    om.y = fmaxf(om.y, 0.0f);
+    const float2 s = make_float2(mufu_sqrt(om.x), mufu_sqrt(om.y));
+    float2 q = fma2(f2(kAcos6), c, f2(kAcos5));
+    q = fma2(q, c, f2(kAcos4));
+    q = fma2(q, c, f2(kAcos3));
+    q = fma2(q, c, f2(kAcos2));
+    q = fma2(q, c, f2(kAcos1));
+    q = fma2(q, c, f2(kAcos0));
+    return mul2(s, q);
+}
+
+// Bin lookup and cubic for one point given its fast theta and q = theta / ANGLE_DIV computed
+// in packed form by the caller: returns D and whether theta is near a bin edge.
+__device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float fq_biased,
+                                           float x, bool& near_edge) {
+    unsigned i = static_cast<unsigned>(__float_as_int(fq_biased) - kTwo23Bits);
+    i = min(i, 10u);  // theta beyond 90 degrees, or anything unexpected, reads the zero entry
+    const float4 c = tab[i];
+    near_edge = fabsf(x - 0.5f * kAngleDiv) > kEdgeBound;
     return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
 }
+
+// Fast directivity of two points (packed) from their cos(theta); `near` receives, in bits 0
+// and 1, whether each point's theta lies within kEdgeMargin of a bin edge (the caller then
+// replaces that point's term through directivity_exact).
+__device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ tab, float2 ct,
+                                                    unsigned& near) {
+    const float2 th = acos2_fast(ct);
+    const float2 fq = __fadd2_ru(mul2(th, f2(kInvAngleDiv)), f2(kTwo23));  // 2^23 + ceil(q)
+    const float2 fi = add2(fq, f2(-kTwo23));                                // ceil(q)
+    const float2 x = fma2(fi, f2(-kAngleDiv), add2(th, f2(kAngleDiv)));    // th - (fi-1) div
+    bool ex, ey;
+    float2 d;
+    d.x = dir_cubic(tab, fq.x, x.x, ex);
+    d.y = dir_cubic(tab, fq.y, x.y, ey);
+    near = (ex ? 1u : 0u) | (ey ? 2u : 0u);
+    return d;
+}
+
+// Directivity of two points with the exact path applied in place (used where the pair is not
+// on the hot loop).
+__device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, float2 ct, float2 dx,
+                                               float2 dy, float2 dz, float nx, float ny, float nz) {
+    unsigned near;
+    float2 d = directivity2_fast(tab, ct, near);
+    if (near & 1u) d.x = directivity_exact(tab, dx.x, dy.x, dz.x, nx, ny, nz);
+    if (near & 2u) d.y = directivity_exact(tab, dx.y, dy.y, dz.y, nx, ny, nz);
+    return d;
+}
+
+// ------------------------------------------------------------------ one pair, scalar
 
 // Weight w and phase reduced to [-pi, pi] for source (a, b) with amplitude `amp` and phase
 // `phase` (layout of PackedSource) at point (px, py, pz).
@@ -64,16 +199,18 @@ __device__ __forceinline__ void pair_terms(const float4& a, const float4& b, flo
     const float dy = py - a.y;
     const float dz = pz - a.z;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const float rinv = rsqrtf(r2);
+    const float rinv = mufu_rsqrt(r2);
     const float r = r2 * rinv;
-    w = amp * rinv * exp2f(b.w * r);
+    w = amp * rinv * mufu_ex2(b.w * r);
     if constexpr (ST == SRC_T4010A1) {
         const float ct = fmaf(b.z, dz, fmaf(b.y, dy, b.x * dx)) * rinv;
-        w *= directivity(tab, acosf(ct));
+        const float2 d = directivity2(tab, make_float2(ct, ct), make_float2(dx, dx),
+                                      make_float2(dy, dy), make_float2(dz, dz), b.x, b.y, b.z);
+        w *= d.x;
     }
     const float ph = fmaf(a.w, r, phase);
-    const float nq = rintf(ph * kInv2Pi);
-    red = fmaf(nq, -kTwoPiLo, fmaf(nq, -kTwoPiHi, ph));
+    const float n = (ph * kInv2Pi + kRoundMagic) - kRoundMagic;
+    red = fmaf(n, -kTwoPiLo, fmaf(n, -kTwoPiHi, ph));
 }
 
 }  // namespace dev

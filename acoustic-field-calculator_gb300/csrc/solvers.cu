@@ -95,9 +95,7 @@ __global__ void build_g_kernel(const PackedSource* __restrict__ src, int64_t n,
     float w, red;
     dev::pair_terms<ST>(s.a, s.b, s.c.x, 0.0f, s_dir, foci[3 * i], foci[3 * i + 1],
                         foci[3 * i + 2], w, red);
-    float sn, cs;
-    __sincosf(red, &sn, &cs);
-    g[i * n + j] = make_float2(w * cs, w * sn);
+    g[i * n + j] = make_float2(w * dev::mufu_cos(red), w * dev::mufu_sin(red));
 }
 
 // inv_den2[j] = 1 / (sum_i |G_ij|)^2

@@ -255,12 +255,11 @@ def run_ours(args):
         step()
     torch.cuda.synchronize()
 
-    mufu = ctypes.c_double()
-    fp32 = ctypes.c_double()
+    rates = (ctypes.c_double * 6)()
     clk = ctypes.c_double()
     nsm = ctypes.c_int32()
-    lib.AFC_MeasureIssueRates(ctypes.byref(mufu), ctypes.byref(fp32), ctypes.byref(clk),
-                              ctypes.byref(nsm))
+    if lib.AFC_MeasurePipeRates(rates, ctypes.byref(clk), ctypes.byref(nsm)) != 0:
+        raise RuntimeError(afc.last_error())
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -311,15 +310,22 @@ def run_ours(args):
     # ---- roofline of the summation kernel (FP32 + MUFU issue)
     clock_summary = clocks.summary()
     sm_mhz = clock_summary.get("sm_mhz") or clk.value / 1e6
-    peak_measured = min(mufu.value / MUFU_PER_EVAL, fp32.value / FP32_PER_EVAL)
+    mufu_names = ["ex2", "rsqrt", "sqrt", "sin", "cos"]
+    mufu_rates = {nm: rates[i] for i, nm in enumerate(mufu_names)}
+    # one of each MUFU op per evaluation: the MUFU pipe's time per eval is the sum of 1/rate
+    mufu_bound = 1.0 / sum(1.0 / r for r in mufu_rates.values())
+    fp32_bound = rates[5] / FP32_PER_EVAL
+    peak_measured = min(mufu_bound, fp32_bound)
     peak_nominal = nsm.value * sm_mhz * 1e6 * min(16 / MUFU_PER_EVAL, 128 / FP32_PER_EVAL)
     roofline = {
         "bound": "fp32+sfu issue (compute)",
         "achieved": per_gpu, "unit": "evals/s",
         "peak": peak_measured, "frac": per_gpu / peak_measured if peak_measured else None,
-        "peak_source": "measured here: MUFU and FFMA microbenchmarks (AFC_MeasureIssueRates), "
-                       f"peak = min(mufu/{MUFU_PER_EVAL}, fp32/{FP32_PER_EVAL})",
-        "mufu_ops_per_s": mufu.value, "fp32_ops_per_s": fp32.value,
+        "peak_source": "measured here with pipe microbenchmarks (AFC_MeasurePipeRates): "
+                       "peak = min(1/sum(1/rate) over ex2, rsqrt, sqrt, sin, cos; "
+                       f"fp32/{FP32_PER_EVAL})",
+        "mufu_ops_per_s": mufu_rates, "fp32_ops_per_s": rates[5],
+        "mufu_bound_evals_per_s": mufu_bound, "fp32_bound_evals_per_s": fp32_bound,
         "calibration_sm_clock_mhz": clk.value / 1e6,
         "peak_nominal_at_sampled_clock": peak_nominal,
         "frac_of_nominal": per_gpu / peak_nominal if peak_nominal else None,

@@ -68,11 +68,11 @@ int32_t AFC_FieldScatterDevice(int32_t source_type, int32_t field_type, int32_t 
                                uint64_t m, void *d_out, void *d_workspace,
                                size_t workspace_bytes, void *stream);
 
-/* Measure, on the current device, the MUFU (special-function) and FP32 FMA result rates
- * [operations/s] with dependency-free microbenchmarks, the SM clock [Hz] while they run, and
- * the SM count.  These are the denominators of the direct summation's roofline. */
-int32_t AFC_MeasureIssueRates(double *mufu_per_s, double *fp32_per_s, double *sm_clock_hz,
-                              int32_t *sm_count);
+/* Measure, on the current device, with dependency-free microbenchmarks, the result rates
+ * [operations/s] of rates[0..4] = MUFU ex2, rsqrt, sqrt, sin, cos and rates[5] = FP32 FMA,
+ * the SM clock [Hz] while they run, and the SM count.  These are the denominators of the
+ * direct summation's roofline. */
+int32_t AFC_MeasurePipeRates(double rates[6], double *sm_clock_hz, int32_t *sm_count);
 
 /* Select the device that calculators and solvers created afterwards on this thread use (the
  * reference's Vulkan calculator always takes the first device, gpu/gpu_calculator.rs:34-37;

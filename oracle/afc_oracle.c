@@ -137,6 +137,22 @@ ORC_EXPORT double oracle_directivity_t4010a1_f64(double theta) {
     return a + (b + ((c + d * x) * x)) * x;
 }
 
+/* ---------------------------------------------------------------- acos rounding */
+
+/* The reference calls the platform libm's acosf.  glibc's acosf (2.39) is not correctly
+ * rounded: it differs by one ulp from the correctly rounded value for a fair share of inputs,
+ * and where theta lies within that ulp of a 10-degree directivity bin edge the bin -- and a
+ * directivity jump of up to 0.164 -- depends on the libm.  Mode 0 (default) uses the
+ * platform acosf like the reference; mode 1 uses acos correctly rounded to f32 (double acos,
+ * then one rounding), which is what the GPU's exact near-edge path computes. */
+static int g_acos_mode = 0;
+
+ORC_EXPORT void oracle_set_acos_mode(int mode) { g_acos_mode = mode; }
+
+static inline float ref_acosf(float c) {
+    return g_acos_mode ? (float)acos((double)c) : acosf(c);
+}
+
 /* ---------------------------------------------------------------- propagate */
 
 /* uniform_medium.rs:111-120 (identical math in macros.rs:17-30), f32, no contraction. */
@@ -146,7 +162,7 @@ static inline void prop_f32(int st, const float *s, float k, float atten, float 
     float dist = sqrtf(dx * dx + dy * dy + dz * dz);
     float amp, phase, d;
     if (st == ORC_SRC_T4010A1) {
-        float theta = acosf((s[3] * dx + s[4] * dy + s[5] * dz) / dist);
+        float theta = ref_acosf((s[3] * dx + s[4] * dy + s[5] * dz) / dist);
         d = oracle_directivity_t4010a1(theta);
         amp = s[6];
         phase = s[7];

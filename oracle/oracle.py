@@ -64,8 +64,32 @@ def lib() -> ctypes.CDLL:
         L.oracle_gs_f64.argtypes = L.oracle_gspat_f64.argtypes
         L.oracle_naive_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, dp]
         L.oracle_max_threads.restype = c_int
+        L.oracle_set_acos_mode.argtypes = [c_int]
         _lib = L
     return _lib
+
+
+ACOS_LIBM, ACOS_CORRECTLY_ROUNDED = 0, 1
+
+
+def set_acos_mode(mode: int) -> None:
+    """0: the platform libm's acosf (what the reference calls); 1: acos correctly rounded to
+    f32 (what the GPU's near-bin-edge path computes).  They differ only where theta lies
+    within one ulp of a directivity bin edge."""
+    lib().oracle_set_acos_mode(mode)
+
+
+class acos_mode:
+    """Context manager that switches the oracle's acos rounding."""
+
+    def __init__(self, mode):
+        self.mode = mode
+
+    def __enter__(self):
+        set_acos_mode(self.mode)
+
+    def __exit__(self, *exc):
+        set_acos_mode(ACOS_LIBM)
 
 
 def _f(a: np.ndarray):

@@ -250,6 +250,37 @@ def test_f32_oracle_within_tolerance_of_f64_on_single_focus():
     assert err < 1e-5
 
 
+def test_libm_and_correctly_rounded_acos_differ_only_at_bin_edges():
+    """glibc's acosf is not correctly rounded.  The two oracle modes may differ only where a
+    pair's theta lies within an ulp of a directivity bin edge; everywhere else they agree
+    exactly."""
+    rng = np.random.default_rng(10)
+    n = 50
+    pos = rng.uniform(-60, 60, (n, 3)).astype(np.float32)
+    pos[:, 2] = rng.uniform(-5, 5, n)
+    rec = W.t4010a1_records(pos, rng.uniform(0.2, 1, n), rng.uniform(-3, 3, n))
+    d = rng.normal(size=(n, 3)) * np.array([0.3, 0.3, 0.0]) + np.array([0, 0, 1.0])
+    rec[:, 3:6] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    k = np.full(n, 0.72, np.float32)
+    a = np.full(n, 0.005, np.float32)
+    lo = np.array([-20, -10, 60], np.float32)
+    hi = np.array([25, 30, 95], np.float32)
+    pts = O.grid_points(3, lo, hi, 1.5, (1, 2, 3))
+    p_libm = O.field_f32(1, rec, k, a, pts)
+    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
+        p_cr = O.field_f32(1, rec, k, a, pts)
+    # a one-ulp theta changes D by ~1e-7 (invisible at this scale); a bin flip by up to 0.164
+    diff = np.nonzero(np.abs(p_libm - p_cr) > 1e-5 * np.max(np.abs(p_cr)))[0]
+    # the points that differ visibly: some pair's theta within 2 ulp of a 10-degree edge
+    div = np.float32(np.float32(math.pi) / np.float32(18))
+    for i in diff:
+        dv = (pts[i] - rec[:, :3]).astype(np.float64)
+        th = np.arccos(np.sum(dv * rec[:, 3:6], axis=1) / np.linalg.norm(dv, axis=1))
+        q = th / float(div)
+        assert np.min(np.abs(q - np.round(q))) < 4e-6
+    assert len(diff) < 0.01 * len(pts)
+
+
 def test_accurate_oracle_close_to_plain():
     w = W.single_focus()
     rng = np.random.default_rng(3)

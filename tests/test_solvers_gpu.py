@@ -79,12 +79,13 @@ def test_gspat_then_field(gpu):
     afc.Optimizer.gs_pat(s, foci, amps)
     z = float(np.mean(foci[:, 2]))
     cen = W.array_center(W.tiled_array(2, 2))
-    area = (afc.GridAreaBuilder().x_range((cen[0] - 100, cen[0] + 100))
-            .y_range((cen[1] - 100, cen[1] + 100)).z_at(z).resolution(1.0).generate())
+    # half a step of padding so that the f32 count ((end - start) / res) as usize + 1 is 201
+    area = (afc.GridAreaBuilder().x_range((cen[0] - 100, cen[0] + 100.5))
+            .y_range((cen[1] - 100, cen[1] + 100.5)).z_at(z).resolution(1.0).generate())
     assert area.get_size() == (201, 201, 1)
     out = afc.GpuCalculator().calculate(s, area, afc.PressureFieldBuffer())
     lo = np.array([cen[0] - 100, cen[1] - 100, z], np.float32)
-    hi = np.array([cen[0] + 100, cen[1] + 100, z], np.float32)
+    hi = np.array([cen[0] + 100.5, cen[1] + 100.5, z], np.float32)
     pts = O.grid_points(2, lo, hi, 1.0, (1, 2, 3))
     ref = O.field_f32(1, s.records().copy(), w.k, w.atten, pts, O.FIELD_PRESSURE)
     assert np.max(np.abs(out - ref)) <= 1e-4 * np.max(ref)
