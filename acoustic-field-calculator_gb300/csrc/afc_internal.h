@@ -24,7 +24,9 @@ inline int source_stride(int st) { return st == SRC_T4010A1 ? 9 : 6; }
 // One source as the field kernels read it (48 bytes, 16-byte aligned):
 //   a = (x, y, z, k)              position [mm], wavenumber [rad/mm]
 //   b = (nx, ny, nz, -alpha*log2e) direction, attenuation as a base-2 exponent per mm
-//   c = (amp, phase, 0, 0)        amplitude, phase [rad]
+//   c = (log2|amp|, phase', amp, phase)
+// The kernels fold the amplitude into the attenuation exponent: A exp(-alpha r) =
+// 2^(log2|A| - alpha log2e r), with the sign of A carried as phase' = phase + pi for A < 0.
 struct __align__(16) PackedSource {
     float4 a, b, c;
 };

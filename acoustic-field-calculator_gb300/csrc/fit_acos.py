@@ -8,7 +8,7 @@ checked against numpy's float64 arccos.  Run: python fit_acos.py
 """
 import numpy as np
 
-LO, HI, DEG = -0.03, 1.0, 6
+LO, HI, DEG = -0.03, 1.0, 5
 
 
 def fit(deg=DEG, lo=LO, hi=HI):

@@ -42,22 +42,20 @@ constexpr int kTwo23Bits = 0x4B000000;
 constexpr float kAngleDiv = 3.14159265358979323846f / 18.0f;
 constexpr float kInvAngleDiv = 18.0f / 3.14159265358979323846f;
 // A fast theta closer than this to a bin edge [rad] takes the exact path.  The fast theta is
-// within ~1e-6 rad of the reference's (rsqrt and FMA rounding in cos(theta), 4e-7 from the
-// polynomial), so 1e-5 leaves a factor of ten.
+// within ~3e-6 rad of the reference's (1.7e-6 from the polynomial, ~1e-6 from rsqrt and FMA
+// rounding in cos(theta)), so 1e-5 leaves a factor of three.
 constexpr float kEdgeMargin = 1.0e-5f;
 constexpr float kEdgeBound = 0.5f * kAngleDiv - kEdgeMargin;
-// cos(theta) is clamped below at -0.03 (theta ~ 91.7 deg, directivity 0 beyond 90 deg).
-constexpr float kCosFloor = -0.03f;
 
-// acos(c) = sqrt(1 - c) * Q(c); Q fitted in fit_acos.py (float32 error <= 4e-7 rad on
-// [-0.03, 1]).
-constexpr float kAcos0 = 1.5707964897155762f;
-constexpr float kAcos1 = -0.21459674835205078f;
-constexpr float kAcos2 = 0.08885793387889862f;
-constexpr float kAcos3 = -0.04917646571993828f;
-constexpr float kAcos4 = 0.027550870552659035f;
-constexpr float kAcos5 = -0.011683782562613487f;
-constexpr float kAcos6 = 0.0024654590524733067f;
+// acos(c) = sqrt(1 - c) * Q(c); Q of degree 5 fitted in fit_acos.py (float32 error <= 1.7e-6
+// rad on [-0.03, 1]; for c in [-1, -0.02] it stays between 1.59 and 2.75 rad, i.e. beyond 90
+// degrees where the directivity is 0, so cos(theta) needs no lower clamp).
+constexpr float kAcos0 = 1.570797085762024f;
+constexpr float kAcos1 = -0.21455863118171692f;
+constexpr float kAcos2 = 0.08815829455852509f;
+constexpr float kAcos3 = -0.04563731327652931f;
+constexpr float kAcos4 = 0.020052572712302208f;
+constexpr float kAcos5 = -0.0045999325811862946f;
 
 // T4010A1 directivity coefficients (t4010a1.rs:18-69) as (a, b, c, d) per bin.  Entry 0
 // (theta == 0) evaluates to 1 like the reference's `0 => 1.0` arm, entries 1 and 2 are the
@@ -134,13 +132,12 @@ static __device__ __noinline__ float directivity_exact(const float4* __restrict_
 
 // Fast theta from cos(theta) for two points.
 __device__ __forceinline__ float2 acos2_fast(float2 ct) {
-    const float2 c = make_float2(fmaxf(ct.x, kCosFloor), fmaxf(ct.y, kCosFloor));
+    const float2 c = ct;
     float2 om = fma2(c, f2(-1.0f), f2(1.0f));  // 1 - c
     om.x = fmaxf(om.x, 0.0f);                  // c rounded above 1 -> theta 0
     om.y = fmaxf(om.y, 0.0f);
     const float2 s = make_float2(mufu_sqrt(om.x), mufu_sqrt(om.y));
-    float2 q = fma2(f2(kAcos6), c, f2(kAcos5));
-    q = fma2(q, c, f2(kAcos4));
+    float2 q = fma2(f2(kAcos5), c, f2(kAcos4));
     q = fma2(q, c, f2(kAcos3));
     q = fma2(q, c, f2(kAcos2));
     q = fma2(q, c, f2(kAcos1));
@@ -148,8 +145,10 @@ __device__ __forceinline__ float2 acos2_fast(float2 ct) {
     return mul2(s, q);
 }
 
-// Bin lookup and cubic for one point given its fast theta and q = theta / ANGLE_DIV computed
-// in packed form by the caller: returns D and whether theta is near a bin edge.
+// Bin lookup and cubic for one point given its fast theta and 2^23 + ceil(theta / ANGLE_DIV)
+// computed in packed form by the caller: returns D and whether theta lies within kEdgeMargin
+// of a bin edge (testing every edge costs fewer instructions than selecting the four where
+// the directivity jumps, and the exact path returns the same D at the others).
 __device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float fq_biased,
                                            float x, bool& near_edge) {
     unsigned i = static_cast<unsigned>(__float_as_int(fq_biased) - kTwo23Bits);
@@ -165,9 +164,9 @@ __device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float
 __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ tab, float2 ct,
                                                     unsigned& near) {
     const float2 th = acos2_fast(ct);
-    const float2 fq = __fadd2_ru(mul2(th, f2(kInvAngleDiv)), f2(kTwo23));  // 2^23 + ceil(q)
-    const float2 fi = add2(fq, f2(-kTwo23));                                // ceil(q)
-    const float2 x = fma2(fi, f2(-kAngleDiv), add2(th, f2(kAngleDiv)));    // th - (fi-1) div
+    const float2 fq = __ffma2_ru(th, f2(kInvAngleDiv), f2(kTwo23));     // 2^23 + ceil(q)
+    const float2 fi = add2(fq, f2(-kTwo23));                             // ceil(q)
+    const float2 x = fma2(fi, f2(-kAngleDiv), add2(th, f2(kAngleDiv)));  // th - (fi-1) div
     bool ex, ey;
     float2 d;
     d.x = dir_cubic(tab, fq.x, x.x, ex);
@@ -189,10 +188,10 @@ __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, f
 
 // ------------------------------------------------------------------ one pair, scalar
 
-// Weight w and phase reduced to [-pi, pi] for source (a, b) with amplitude `amp` and phase
-// `phase` (layout of PackedSource) at point (px, py, pz).
+// Weight w and phase reduced to [-pi, pi] for source (a, b) with log2|amplitude| `la` and
+// phase `phase` (sign of the amplitude folded in, layout of PackedSource) at point (px, py, pz).
 template <int ST>
-__device__ __forceinline__ void pair_terms(const float4& a, const float4& b, float amp,
+__device__ __forceinline__ void pair_terms(const float4& a, const float4& b, float la,
                                            float phase, const float4* __restrict__ tab, float px,
                                            float py, float pz, float& w, float& red) {
     const float dx = px - a.x;
@@ -201,7 +200,7 @@ __device__ __forceinline__ void pair_terms(const float4& a, const float4& b, flo
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float rinv = mufu_rsqrt(r2);
     const float r = r2 * rinv;
-    w = amp * rinv * mufu_ex2(b.w * r);
+    w = rinv * mufu_ex2(fmaf(b.w, r, la));
     if constexpr (ST == SRC_T4010A1) {
         const float ct = fmaf(b.z, dz, fmaf(b.y, dy, b.x * dx)) * rinv;
         const float2 d = directivity2(tab, make_float2(ct, ct), make_float2(dx, dx),

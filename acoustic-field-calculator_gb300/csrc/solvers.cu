@@ -93,8 +93,9 @@ __global__ void build_g_kernel(const PackedSource* __restrict__ src, int64_t n,
     if (j >= n) return;
     const PackedSource s = src[j];
     float w, red;
-    dev::pair_terms<ST>(s.a, s.b, s.c.x, 0.0f, s_dir, foci[3 * i], foci[3 * i + 1],
-                        foci[3 * i + 2], w, red);
+    // the phases are zeroed before G is built (gs_pat.rs:39-41): phase' is pi for A < 0
+    dev::pair_terms<ST>(s.a, s.b, s.c.x, s.c.z < 0.f ? 3.14159265358979323846f : 0.0f, s_dir,
+                        foci[3 * i], foci[3 * i + 1], foci[3 * i + 2], w, red);
     g[i * n + j] = make_float2(w * dev::mufu_cos(red), w * dev::mufu_sin(red));
 }
 
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(kIterThreads)
                       const float* __restrict__ amps, int64_t n, int64_t m, int repeat, float2* q,
                       float2* p, float* __restrict__ out) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) q[j] = make_float2(src[j].c.x, 0.f);
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) q[j] = make_float2(src[j].c.z, 0.f);
     __syncthreads();
     for (int it = 0; it < repeat; ++it) {
         // gamma = G q, p = gamma / |gamma| * p0
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(kIterThreads)
                 acc.x += t.x;
                 acc.y += t.y;
             }
-            const float s = src[j].c.x / hypotf(acc.x, acc.y);
+            const float s = src[j].c.z / hypotf(acc.x, acc.y);
             q[j] = make_float2(acc.x * s, acc.y * s);
         }
         __syncthreads();
