@@ -111,7 +111,7 @@ NEW_EXPORTS = [
     "AFC_GetLastError", "AFC_ClearLastError",
     "AFC_GridDescFromArea", "AFC_FieldWorkspaceBytes", "AFC_FieldGridDevice",
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
-    "AFC_MeasurePipeRates", "AFC_SetDevice",
+    "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
 ]
 
 
@@ -240,3 +240,7 @@ def __init_new():
     AFC_DLL.AFC_MeasurePipeRates.restype = c_int32
     AFC_DLL.AFC_SetDevice.argtypes = [c_int32]
     AFC_DLL.AFC_SetDevice.restype = c_int32
+    AFC_DLL.AFC_FieldGridDeviceNoAlloc.argtypes = [c_int32, c_int32, c_int32, c_void_p, c_void_p,
+                                                   c_void_p, c_uint64, POINTER(GridDesc),
+                                                   c_void_p, c_void_p]
+    AFC_DLL.AFC_FieldGridDeviceNoAlloc.restype = c_int32

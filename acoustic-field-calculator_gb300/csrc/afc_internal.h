@@ -55,6 +55,9 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
                          const PointSet& ps, void* out, cudaStream_t s);
 
+// Record `msg` as this thread's last error (read back by AFC_GetLastError).
+void set_error_message(const char* msg);
+
 // Kernels launched by this library since load (the bench reports the delta).
 extern std::atomic<uint64_t> g_launches;
 inline void count_launch(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }

@@ -505,6 +505,8 @@ int32_t device_field(int32_t st, int32_t ft, int32_t sum, const float* d_sources
 
 }  // namespace
 
+void afc::set_error_message(const char* msg) { t_last_error = msg ? msg : ""; }
+
 extern "C" {
 
 // ------------------------------------------------------------------ errors

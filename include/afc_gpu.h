@@ -82,6 +82,25 @@ int32_t AFC_SetDevice(int32_t device);
 /* Number of CUDA devices visible to this library (0 when none or the driver is unusable). */
 int32_t AFC_CudaDeviceCount(void);
 
+/* Allocation-free AFC_FieldGridDevice.  This entry point has no counterpart in the reference.
+ *
+ * For callers that cannot allocate GPU memory while they run: a real-time loop driving a
+ * transducer array that must not block on the allocator or fail on memory mid-run, a host
+ * that has handed the device's memory to its own pool, a plugin whose host forbids
+ * allocation inside callbacks.  Instead of a caller-supplied workspace it uses a fixed
+ * scratch array of AFC_NOALLOC_MAX_SOURCES packed sources (768 KiB) that the library
+ * reserves on every GPU it is loaded on, for the life of the process; inputs and output are
+ * the caller's, as for AFC_FieldGridDevice.  More sources than AFC_NOALLOC_MAX_SOURCES are
+ * rejected with AFC_ERR_TOO_LARGE.  The first call on each device looks the scratch address
+ * up (make it before capturing the stream into a graph).  All calls share the one scratch
+ * array, so calls whose GPU work overlaps (unordered streams) race; order them on one stream.
+ * It calls no allocator. */
+#define AFC_NOALLOC_MAX_SOURCES 16384
+int32_t AFC_FieldGridDeviceNoAlloc(int32_t source_type, int32_t field_type, int32_t sum_mode,
+                                   const float *d_sources, const float *d_wavenums,
+                                   const float *d_attens, uint64_t n, const AfcGridDesc *grid,
+                                   void *d_out, void *stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t AFC_KernelLaunchCount(void);
 
