@@ -206,6 +206,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ------------------------------------------------------------------ ranks
+
+def max_over_ranks(seconds: float, dist, device) -> float:
+    """The slowest rank's time (every rank gets it); `dist` None means one process."""
+    if dist is None:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units processed by all ranks (replicas: each rank does the same work) per second."""
+    return units_per_rank * world / seconds
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def run_ours(args):
@@ -281,11 +299,8 @@ def run_ours(args):
             dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = sum(step_ms) * 1e-3
-    if dist:
-        tt = torch.tensor([total_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt.item())
-    value = evals * args.steps * world / total_s
+    total_s = max_over_ranks(total_s, dist, dev)
+    value = whole_job_rate(evals * args.steps, world, total_s)
     per_gpu = evals * args.steps / total_s
 
     # ---- end-to-end arm through AFC_Calculate (host buffers)
@@ -300,10 +315,7 @@ def run_ours(args):
     for _ in range(e2e_steps):
         calc.calculate_raw(system, area, field)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist:
-        tt = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(e2e_s, dist, dev)
     h2d = w.n * (9 + 2) * 4
     d2h = m * 8
 
