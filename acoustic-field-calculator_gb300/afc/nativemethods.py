@@ -112,6 +112,8 @@ NEW_EXPORTS = [
     "AFC_GridDescFromArea", "AFC_FieldWorkspaceBytes", "AFC_FieldGridDevice",
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
     "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
+    "AFC_MultiPatternWorkspaceBytes", "AFC_MultiPatternBuildG", "AFC_MultiPatternApply",
+    "AFC_MultiPatternStatus", "AFC_MultiPatternDirect",
 ]
 
 
@@ -244,3 +246,19 @@ def __init_new():
                                                    c_void_p, c_uint64, POINTER(GridDesc),
                                                    c_void_p, c_void_p]
     AFC_DLL.AFC_FieldGridDeviceNoAlloc.restype = c_int32
+    AFC_DLL.AFC_MultiPatternWorkspaceBytes.argtypes = [c_uint64, c_uint64, c_uint64, c_int32]
+    AFC_DLL.AFC_MultiPatternWorkspaceBytes.restype = c_size_t
+    AFC_DLL.AFC_MultiPatternBuildG.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                               c_uint64, c_void_p, c_uint64, c_uint64, c_void_p,
+                                               c_size_t, c_void_p]
+    AFC_DLL.AFC_MultiPatternBuildG.restype = c_int32
+    AFC_DLL.AFC_MultiPatternApply.argtypes = [c_int32, c_void_p, c_void_p, c_uint64, c_uint64,
+                                              c_uint64, c_void_p, c_void_p, c_size_t, c_void_p]
+    AFC_DLL.AFC_MultiPatternApply.restype = c_int32
+    AFC_DLL.AFC_MultiPatternStatus.argtypes = [c_int32, c_uint64, c_uint64, c_uint64, c_void_p,
+                                               c_void_p]
+    AFC_DLL.AFC_MultiPatternStatus.restype = c_int32
+    AFC_DLL.AFC_MultiPatternDirect.argtypes = [c_int32, c_void_p, c_void_p, c_void_p, c_uint64,
+                                               c_void_p, c_uint64, c_void_p, c_void_p, c_uint64,
+                                               c_void_p, c_void_p, c_size_t, c_void_p]
+    AFC_DLL.AFC_MultiPatternDirect.restype = c_int32

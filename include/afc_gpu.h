@@ -68,6 +68,39 @@ int32_t AFC_FieldScatterDevice(int32_t source_type, int32_t field_type, int32_t 
                                uint64_t m, void *d_out, void *d_workspace,
                                size_t workspace_bytes, void *stream);
 
+/* ---- many phase patterns on one geometry (no counterpart in the reference: the reference
+ * evaluates one pattern per AFC_Calculate) ----
+ *
+ * P (m points x K patterns, complex, row-major: P[i][k] at d_out[2 (i K + k)]) = G Q with
+ * G_ij the field of source j at point i for unit amplitude and zero phase and
+ * Q_jk = amps[k][j] exp(i phases[k][j]).  AFC_MultiPatternBuildG builds G once per geometry into
+ * the workspace; AFC_MultiPatternApply evaluates any number of pattern sets against it on the
+ * tensor cores.  Precision AFC_PRECISION_BF16X3: G and Q split into bf16 hi + lo parts,
+ * hi*hi + hi*lo + lo*hi accumulated in FP32; AFC_PRECISION_FP16: one FP16 product with each
+ * row of G scaled by a power of two. */
+enum { AFC_PRECISION_BF16X3 = 1, AFC_PRECISION_FP16 = 2 };
+size_t AFC_MultiPatternWorkspaceBytes(uint64_t n, uint64_t m, uint64_t patterns,
+                                      int32_t precision);
+int32_t AFC_MultiPatternBuildG(int32_t source_type, int32_t precision, const float *d_sources,
+                               const float *d_wavenums, const float *d_attens, uint64_t n,
+                               const float *d_points, uint64_t m, uint64_t patterns,
+                               void *d_workspace, size_t workspace_bytes, void *stream);
+int32_t AFC_MultiPatternApply(int32_t precision, const float *d_amps, const float *d_phases,
+                              uint64_t n, uint64_t m, uint64_t patterns, float *d_out,
+                              void *d_workspace, size_t workspace_bytes, void *stream);
+/* 0 if the last AFC_MultiPatternApply in this workspace completed, else the code of the
+ * tensor-core pipeline stage whose bounded wait expired (1 loader, 2 MMA, 3 epilogue).
+ * Synchronises the stream. */
+int32_t AFC_MultiPatternStatus(int32_t precision, uint64_t n, uint64_t m, uint64_t patterns,
+                               void *d_workspace, void *stream);
+/* The same P by FP32 direct summation, one field evaluation per pattern, written pattern-major
+ * (P[i][k] at d_out[2 (k m + i)]); workspace of 2 * AFC_FieldWorkspaceBytes(n) bytes. */
+int32_t AFC_MultiPatternDirect(int32_t source_type, const float *d_sources,
+                               const float *d_wavenums, const float *d_attens, uint64_t n,
+                               const float *d_points, uint64_t m, const float *d_amps,
+                               const float *d_phases, uint64_t patterns, float *d_out,
+                               void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Measure, on the current device, with dependency-free microbenchmarks, the result rates
  * [operations/s] of rates[0..4] = MUFU ex2, rsqrt, sqrt, sin, cos and rates[5] = FP32 FMA,
  * the SM clock [Hz] while they run, and the SM count.  These are the denominators of the

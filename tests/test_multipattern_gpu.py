@@ -1,0 +1,99 @@
+"""Many patterns on one geometry: P = G Q on the tensor cores (split BF16 and row-scaled FP16)
+and by FP32 direct summation, against P computed in float64 from the oracle's G.
+
+Bars (max |P - P64| / max |P64|): split BF16 <= 1e-4, FP32 direct <= 1e-4, FP16 <= 2e-3
+(11-bit inputs)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+BF16X3, FP16 = 1, 2
+
+
+def _problem(seed, n_tiles, m, K):
+    rng = np.random.default_rng(seed)
+    pos = W.tiled_array(*n_tiles)
+    cen = W.array_center(pos)
+    pts = W.scatter_box(seed + 7, m, cen[:2], box=(120.0, 120.0), z=(60.0, 180.0))
+    n = len(pos)
+    src = W.t4010a1_records(pos, 1.0, 0.0)
+    k = np.full(n, W.wavenumber(), np.float32)
+    a = np.full(n, 1.15e-2, np.float32)
+    amps = rng.uniform(0.5, 1.0, (K, n)).astype(np.float32)
+    phases = rng.uniform(0, 2 * np.pi, (K, n)).astype(np.float32)
+    return src, k, a, pts, amps, phases
+
+
+def _p64(src, k, a, pts, amps, phases):
+    g = O.build_g_f64(1, src, k, a, pts)  # unit amplitude, zero phase
+    q = amps.astype(np.float64) * np.exp(1j * phases.astype(np.float64))
+    return g @ q.T  # m x K
+
+
+def _run(afc, torch, prec, src, k, a, pts, amps, phases):
+    n, m, K = len(k), len(pts), len(amps)
+    dev = "cuda"
+    d_src = torch.from_numpy(src.reshape(-1)).to(dev)
+    d_k = torch.from_numpy(k).to(dev)
+    d_a = torch.from_numpy(a).to(dev)
+    d_pts = torch.from_numpy(pts.reshape(-1)).to(dev)
+    d_amps = torch.from_numpy(amps.reshape(-1)).to(dev)
+    d_ph = torch.from_numpy(phases.reshape(-1)).to(dev)
+    wsb = afc.DLL.AFC_MultiPatternWorkspaceBytes(n, m, K, prec)
+    ws = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
+    base = (ws.data_ptr() + 255) // 256 * 256
+    out = torch.zeros(2 * m * K, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    rc = afc.DLL.AFC_MultiPatternBuildG(1, prec, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                        n, d_pts.data_ptr(), m, K, base, wsb, st)
+    assert rc == 0, afc.last_error()
+    rc = afc.DLL.AFC_MultiPatternApply(prec, d_amps.data_ptr(), d_ph.data_ptr(), n, m, K,
+                                       out.data_ptr(), base, wsb, st)
+    assert rc == 0, afc.last_error()
+    assert afc.DLL.AFC_MultiPatternStatus(prec, n, m, K, base, st) == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(np.complex64).reshape(m, K)
+
+
+def _direct(afc, torch, src, k, a, pts, amps, phases):
+    n, m, K = len(k), len(pts), len(amps)
+    dev = "cuda"
+    t = [torch.from_numpy(x.reshape(-1)).to(dev) for x in (src, k, a, pts, amps, phases)]
+    wsb = 2 * afc.DLL.AFC_FieldWorkspaceBytes(n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    out = torch.zeros(2 * m * K, dtype=torch.float32, device=dev)
+    rc = afc.DLL.AFC_MultiPatternDirect(1, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), n,
+                                        t[3].data_ptr(), m, t[4].data_ptr(), t[5].data_ptr(), K,
+                                        out.data_ptr(), ws.data_ptr(), wsb,
+                                        torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, afc.last_error()
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(np.complex64).reshape(K, m).T
+
+
+def _errs(p, ref):
+    return (float(np.max(np.abs(p - ref)) / np.max(np.abs(ref))),
+            float(np.linalg.norm(p - ref) / np.linalg.norm(ref)))
+
+
+@pytest.mark.parametrize("K", [64, 128, 200])
+def test_multipattern_precisions_vs_f64(gpu, K):
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    src, k, a, pts, amps, phases = _problem(50 + K, (1, 1), 1000, K)
+    ref = _p64(src, k, a, pts, amps, phases)
+    p_bf = _run(afc, torch, BF16X3, src, k, a, pts, amps, phases)
+    p_h = _run(afc, torch, FP16, src, k, a, pts, amps, phases)
+    p_d = _direct(afc, torch, src, k, a, pts, amps, phases)
+    e_bf, e_h, e_d = _errs(p_bf, ref), _errs(p_h, ref), _errs(p_d, ref)
+    print(f"K={K}: split-BF16 max {e_bf[0]:.2e} rel-L2 {e_bf[1]:.2e} | FP16 max {e_h[0]:.2e} "
+          f"rel-L2 {e_h[1]:.2e} | FP32 direct max {e_d[0]:.2e} rel-L2 {e_d[1]:.2e}")
+    assert e_bf[0] <= 1e-4
+    assert e_d[0] <= 1e-4
+    assert e_h[0] <= 2e-3
