@@ -89,6 +89,14 @@ class GridDesc(Structure):
                 ("res", c_float)]
 
 
+class FieldJob(Structure):
+    """NEW: AfcFieldJob of include/afc_gpu.h."""
+    _fields_ = [("n_sources", c_uint64), ("d_sources", c_void_p), ("d_wavenums", c_void_p),
+                ("d_attens", c_void_p), ("field_type", c_int32), ("is_grid", c_int32),
+                ("grid", GridDesc), ("d_points", c_void_p), ("n_points", c_uint64),
+                ("d_out", c_void_p)]
+
+
 AFC_DLL = None
 
 # Every export of include/afccapi.h and include/afc_gpu.h (checked by the symbol test).
@@ -113,7 +121,8 @@ NEW_EXPORTS = [
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
     "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
     "AFC_MultiPatternWorkspaceBytes", "AFC_MultiPatternBuildG", "AFC_MultiPatternApply",
-    "AFC_MultiPatternStatus", "AFC_MultiPatternDirect",
+    "AFC_MultiPatternStatus", "AFC_MultiPatternDirect", "AFC_BatchCreate", "AFC_BatchRun",
+    "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchFree",
 ]
 
 
@@ -262,3 +271,15 @@ def __init_new():
                                                c_void_p, c_uint64, c_void_p, c_void_p, c_uint64,
                                                c_void_p, c_void_p, c_size_t, c_void_p]
     AFC_DLL.AFC_MultiPatternDirect.restype = c_int32
+    AFC_DLL.AFC_BatchCreate.argtypes = [c_int32, POINTER(FieldJob), c_uint64, c_int32,
+                                        POINTER(c_void_p), c_void_p]
+    AFC_DLL.AFC_BatchCreate.restype = c_int32
+    AFC_DLL.AFC_BatchRun.argtypes = [c_void_p, c_void_p]
+    AFC_DLL.AFC_BatchRun.restype = c_int32
+    AFC_DLL.AFC_BatchRunOneByOne.argtypes = [c_void_p, c_void_p]
+    AFC_DLL.AFC_BatchRunOneByOne.restype = c_int32
+    AFC_DLL.AFC_BatchDescribe.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32),
+                                          POINTER(c_uint64), POINTER(c_double)]
+    AFC_DLL.AFC_BatchDescribe.restype = c_int32
+    AFC_DLL.AFC_BatchFree.argtypes = [c_void_p]
+    AFC_DLL.AFC_BatchFree.restype = None

@@ -55,6 +55,9 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
                          const PointSet& ps, void* out, cudaStream_t s);
 
+// Streaming multiprocessors of the current device (cached after the first query).
+int num_sms();
+
 // Record `msg` as this thread's last error (read back by AFC_GetLastError).
 void set_error_message(const char* msg);
 

@@ -1,0 +1,300 @@
+// Per-block body of the direct summation, shared by the single-job kernel
+// (field_kernels.cu) and the persistent batched kernel (batch.cu): shared-memory source tiles,
+// packed point pairs, the near-bin-edge correction, and the field-transform epilogue.  See
+// field_kernels.cu for the schedule and propagate.cuh for the per-pair math.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "afc_internal.h"
+#include "propagate.cuh"
+
+namespace afc {
+namespace fb {
+
+using namespace dev;
+
+constexpr int kThreads = 256;  // threads per block
+constexpr int kTile = 256;     // sources per shared-memory tile
+
+// PackedSource j from the ABI records (T4010A1: 9 floats, sphere: 6), wavenumbers and
+// attenuations; the amplitude goes into the exponent as log2|A| and its sign into the phase.
+__device__ __forceinline__ PackedSource pack_source(int st, const float* __restrict__ raw,
+                                                   const float* __restrict__ k,
+                                                   const float* __restrict__ atten, int64_t j) {
+    PackedSource p;
+    float amp, phase;
+    if (st == SRC_T4010A1) {
+        const float* s = raw + 9 * j;
+        p.a = make_float4(s[0], s[1], s[2], k[j]);
+        p.b = make_float4(s[3], s[4], s[5], -atten[j] * kLog2e);
+        amp = s[6];
+        phase = s[7];
+    } else {
+        const float* s = raw + 6 * j;
+        p.a = make_float4(s[0], s[1], s[2], k[j]);
+        p.b = make_float4(0.f, 0.f, 0.f, -atten[j] * kLog2e);
+        amp = s[3];
+        phase = s[4];
+    }
+    const float ph = amp < 0.f ? phase + 3.14159265358979323846f : phase;
+    p.c = make_float4(log2f(fabsf(amp)), ph, amp, phase);
+    return p;
+}
+
+// Shared-memory image of one source: five float4 of duplicated scalars and -n0.s.
+//   v0 = (-x, -x, -y, -y)   v1 = (-z, -z, k, k)   v2 = (nx, nx, ny, ny)
+//   v3 = (nz, nz, a2, a2)   v4 = (la, la, ph, ph)   ns = (-n0.s, -n0.s)
+// a2 = -alpha log2(e), la = log2|A|, ph = phase (+ pi for A < 0), n0 = direction of source 0.
+struct SmemTile {
+    float4 v0[kTile], v1[kTile], v2[kTile], v3[kTile], v4[kTile];
+    float2 ns[kTile];
+    float4 dir[kDirTableSize];
+};
+
+// Neumaier's compensated addition: sum + v with the lost low-order part added to comp.
+__device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
+    const float t = __fadd_rn(sum, v);
+    if (fabsf(sum) >= fabsf(v)) {
+        comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(sum, t), v));
+    } else {
+        comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(v, t), sum));
+    }
+    sum = t;
+}
+
+// Coordinates of grid point p, bit-identical to the reference's o + (n as f32 * res).
+__device__ __forceinline__ void grid_point(const GridDev& g, int64_t p, float& x, float& y,
+                                           float& z) {
+    const int64_t i0 = p % g.count[0];
+    const int64_t q = p / g.count[0];
+    const int64_t i1 = q % g.count[1];
+    const int64_t i2 = q / g.count[1];
+    float v[3] = {g.origin[0], g.origin[1], g.origin[2]};
+    const int64_t idx[3] = {i0, i1, i2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (g.count[k] > 1) {
+            const int a = g.axis[k];
+            const float o = a == 0 ? g.origin[0] : (a == 1 ? g.origin[1] : g.origin[2]);
+            const float c = __fadd_rn(o, __fmul_rn(__ll2float_rn(idx[k]), g.res));
+            if (a == 0) v[0] = c;
+            else if (a == 1) v[1] = c;
+            else v[2] = c;
+        }
+    }
+    x = v[0];
+    y = v[1];
+    z = v[2];
+}
+
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+__device__ __forceinline__ float& lane_of(float2& v, int hi) { return hi ? v.y : v.x; }
+
+// Reduced phase phi + k r - n 2pi in [-pi, pi] for two points, with 2 pi rounded to f32:
+// the reduction error n (2 pi - float(2 pi)) is below 1.2e-5 rad for n < 70 turns (distances
+// up to ~600 mm at 40 kHz), comparable to the rounding of phi + k r itself in the reference.
+__device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase) {
+    const float2 ph = fma2(k, r, phase);
+    const float2 nq = add2(fma2(ph, f2(kInv2Pi), f2(kRoundMagic)), f2(-kRoundMagic));
+    return fma2(nq, f2(-kTwoPiHi), ph);
+}
+
+// Correction for one point whose fast theta fell next to a bin edge: recompute the pair with
+// the same fast operations (UD: cos(theta) from the shared direction) and return
+// w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators.  Everything
+// passes by value so that the caller's accumulators stay in registers.
+template <bool UD>
+__device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
+                                               float4 v2, float4 v3, float4 v4, float2 ns,
+                                               float3 n0, float np, float px, float py, float pz) {
+    const float dx = px + v0.x, dy = py + v0.z, dz = pz + v1.x;
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float rinv = mufu_rsqrt(r2);
+    const float r = r2 * rinv;
+    const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
+    float ct, nx, ny, nz;
+    if constexpr (UD) {
+        ct = (np + ns.x) * rinv;
+        nx = n0.x;
+        ny = n0.y;
+        nz = n0.z;
+    } else {
+        ct = fmaf(v3.x, dz, fmaf(v2.z, dy, v2.x * dx)) * rinv;
+        nx = v2.x;
+        ny = v2.z;
+        nz = v3.x;
+    }
+    unsigned near;
+    const float d_fast = directivity2_fast(tab, make_float2(ct, ct), near).x;
+    const float d_exact = directivity_exact(tab, dx, dy, dz, nx, ny, nz);
+    const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
+    const float corr = w0 * (d_exact - d_fast);
+    return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
+}
+
+// The PAIRS point pairs of one thread against shared-memory source j.
+template <int ST, int SUM, int PAIRS, bool UD>
+__device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, float3 n0,
+                                                  float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
+                                                  float2 (&PZ)[PAIRS], float2 (&NP)[PAIRS],
+                                                  float2 (&RE)[PAIRS], float2 (&IM)[PAIRS],
+                                                  float2 (&CRE)[PAIRS], float2 (&CIM)[PAIRS]) {
+    const float4 v0 = sm.v0[j], v1 = sm.v1[j], v3 = sm.v3[j], v4 = sm.v4[j];
+    float4 v2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 ns = f2(0.f);
+    if constexpr (ST == SRC_T4010A1) {
+        if constexpr (UD) ns = sm.ns[j];
+        else v2 = sm.v2[j];
+    }
+    unsigned near_mask = 0;
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        const float2 dx = add2(PX[q], lo2(v0));
+        const float2 dy = add2(PY[q], hi2(v0));
+        const float2 dz = add2(PZ[q], lo2(v1));
+        const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const float2 rinv = make_float2(mufu_rsqrt(r2.x), mufu_rsqrt(r2.y));
+        const float2 r = mul2(r2, rinv);
+        const float2 ea = fma2(hi2(v3), r, lo2(v4));
+        float2 w = mul2(rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
+        if constexpr (ST == SRC_T4010A1) {
+            float2 ct;
+            if constexpr (UD) ct = mul2(add2(NP[q], ns), rinv);
+            else ct = mul2(fma2(lo2(v3), dz, fma2(hi2(v2), dy, mul2(lo2(v2), dx))), rinv);
+            unsigned near;
+            w = mul2(w, directivity2_fast(sm.dir, ct, near));
+            near_mask |= near << (2 * q);
+        }
+        const float2 red = reduce_phase2(hi2(v1), r, hi2(v4));
+        const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
+        const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
+        if constexpr (SUM == SUM_PLAIN) {
+            RE[q] = fma2(w, cs, RE[q]);
+            IM[q] = fma2(w, sn, IM[q]);
+        } else {
+            const float2 tr = mul2(w, cs), ti = mul2(w, sn);
+            neumaier_add(RE[q].x, CRE[q].x, tr.x);
+            neumaier_add(RE[q].y, CRE[q].y, tr.y);
+            neumaier_add(IM[q].x, CIM[q].x, ti.x);
+            neumaier_add(IM[q].y, CIM[q].y, ti.y);
+        }
+    }
+    if constexpr (ST == SRC_T4010A1) {
+        if (near_mask) {
+#pragma unroll
+            for (int k = 0; k < 2 * PAIRS; ++k) {
+                if (near_mask & (1u << k)) {
+                    const int q = k >> 1, h = k & 1;
+                    const float2 c = edge_correction<UD>(sm.dir, v0, v1, v2, v3, v4, ns, n0,
+                                                         lane_of(NP[q], h), lane_of(PX[q], h),
+                                                         lane_of(PY[q], h), lane_of(PZ[q], h));
+                    if constexpr (SUM == SUM_PLAIN) {
+                        lane_of(RE[q], h) += c.x;
+                        lane_of(IM[q], h) += c.y;
+                    } else {
+                        neumaier_add(lane_of(RE[q], h), lane_of(CRE[q], h), c.x);
+                        neumaier_add(lane_of(IM[q], h), lane_of(CIM[q], h), c.y);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// One block of 2*PAIRS*kThreads observation points starting at point `first`: stage the n
+// sources tile by tile into `sm` (its dir table must already be filled), accumulate, apply
+// the field transform and store.  `grid` selects generated grid points or explicit ones.
+template <int ST, int SUM, int PAIRS>
+__device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* __restrict__ src,
+                                             int64_t n, bool grid, const GridDev& g,
+                                             const float* __restrict__ pts, int64_t m,
+                                             int64_t first, int field, void* __restrict__ out) {
+    constexpr int kPPT = 2 * PAIRS;
+    const int64_t base = first + threadIdx.x;
+    float2 PX[PAIRS], PY[PAIRS], PZ[PAIRS], NP[PAIRS];
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+#pragma unroll
+    for (int k = 0; k < kPPT; ++k) {
+        int64_t p = base + static_cast<int64_t>(k) * kThreads;
+        if (p >= m) p = m - 1;  // computed but never stored
+        float x, y, z;
+        if (grid) {
+            grid_point(g, p, x, y, z);
+        } else {
+            x = __ldg(pts + 3 * p);
+            y = __ldg(pts + 3 * p + 1);
+            z = __ldg(pts + 3 * p + 2);
+        }
+        lane_of(PX[k >> 1], k & 1) = x;
+        lane_of(PY[k >> 1], k & 1) = y;
+        lane_of(PZ[k >> 1], k & 1) = z;
+    }
+    // direction of source 0: the reference direction of the shared-direction path
+    float3 n0 = make_float3(0.f, 0.f, 0.f);
+    if (ST == SRC_T4010A1 && n > 0) {
+        const float4 b0 = src[0].b;
+        n0 = make_float3(b0.x, b0.y, b0.z);
+    }
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        NP[q] = fma2(f2(n0.z), PZ[q], fma2(f2(n0.y), PY[q], mul2(f2(n0.x), PX[q])));
+        RE[q] = f2(0.f);
+        IM[q] = f2(0.f);
+        CRE[q] = f2(0.f);
+        CIM[q] = f2(0.f);
+    }
+
+    for (int64_t t0 = 0; t0 < n; t0 += kTile) {
+        const int cnt = static_cast<int>((n - t0) < kTile ? (n - t0) : kTile);
+        __syncthreads();
+        bool same_dir = true;
+        for (int j = threadIdx.x; j < cnt; j += kThreads) {
+            const PackedSource s = src[t0 + j];
+            sm.v0[j] = make_float4(-s.a.x, -s.a.x, -s.a.y, -s.a.y);
+            sm.v1[j] = make_float4(-s.a.z, -s.a.z, s.a.w, s.a.w);
+            sm.v2[j] = make_float4(s.b.x, s.b.x, s.b.y, s.b.y);
+            sm.v3[j] = make_float4(s.b.z, s.b.z, s.b.w, s.b.w);
+            sm.v4[j] = make_float4(s.c.x, s.c.x, s.c.y, s.c.y);
+            const float ns = fmaf(n0.z, s.a.z, fmaf(n0.y, s.a.y, n0.x * s.a.x));
+            sm.ns[j] = f2(-ns);
+            same_dir = same_dir && s.b.x == n0.x && s.b.y == n0.y && s.b.z == n0.z;
+        }
+        const bool tile_same_dir = __syncthreads_and(same_dir);
+        if (ST == SRC_T4010A1 && tile_same_dir) {
+#pragma unroll 1
+            for (int j = 0; j < cnt; ++j)
+                accumulate_source<ST, SUM, PAIRS, true>(sm, j, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < cnt; ++j)
+                accumulate_source<ST, SUM, PAIRS, false>(sm, j, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+        }
+    }
+
+#pragma unroll
+    for (int k = 0; k < kPPT; ++k) {
+        const int64_t p = base + static_cast<int64_t>(k) * kThreads;
+        if (p >= m) break;
+        float vr = lane_of(RE[k >> 1], k & 1);
+        float vi = lane_of(IM[k >> 1], k & 1);
+        if constexpr (SUM == SUM_COMPENSATED) {
+            vr = __fadd_rn(vr, lane_of(CRE[k >> 1], k & 1));
+            vi = __fadd_rn(vi, lane_of(CIM[k >> 1], k & 1));
+        }
+        if (field == FIELD_COMPLEX) {
+            reinterpret_cast<float2*>(out)[p] = make_float2(vr, vi);
+        } else {
+            // norm_sqr = re*re + im*im without contraction (pressure_field.rs:35-37)
+            const float ns = __fadd_rn(__fmul_rn(vr, vr), __fmul_rn(vi, vi));
+            reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
+        }
+    }
+}
+
+}  // namespace fb
+}  // namespace afc

@@ -216,3 +216,64 @@ def gspat_request(rng: np.random.Generator, n_foci: int, tiles=(2, 2), z=(100.0,
     k, a = _uniform_k_atten(len(pos), 0.0)
     return Workload(f"gspat_{len(pos)}src_{n_foci}foci", 1, src, k, a, points=foci,
                     field_type=0), foci, amps
+
+
+# transducer counts of the batched-job mix and the tilings that give them
+JOB_TILINGS = {249: (1, 1), 498: (2, 1), 996: (2, 2), 2490: (5, 2)}
+
+
+@dataclasses.dataclass
+class BatchJob:
+    """One job of a batch: its sources (ABI records), and either a 2-D XY grid slice or a count
+    of scatter points drawn uniformly over the array from `points_seed`."""
+
+    sources: np.ndarray
+    k: np.ndarray
+    atten: np.ndarray
+    field_type: int
+    grid: GridSpec | None
+    n_points: int
+    points_seed: int
+    box_lo: tuple
+    box_hi: tuple
+
+    @property
+    def n(self):
+        return len(self.k)
+
+
+def batch_jobs(seed: int = 3, n_jobs: int = 2048, m_range=(1e3, 1e6),
+               counts=(249, 498, 996, 2490), alpha: float = 1.15e-2):
+    """The uneven-job mix: transducer count uniform over `counts` (array tilings), point count
+    log-uniform in `m_range`, half the jobs 2-D XY grid slices at 0.5-2 mm spacing (z 50-200 mm
+    over the array centre), half scatter sets in a box over the array; random phases and
+    amplitudes; field type uniform over pressure / power / complex."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(n_jobs):
+        n = int(rng.choice(counts))
+        pos = tiled_array(*JOB_TILINGS[n])
+        cen = array_center(pos)
+        amp, phase = random_pattern(rng, n)
+        src = t4010a1_records(pos, amp, phase)
+        k, a = _uniform_k_atten(n, alpha)
+        m = int(round(math.exp(rng.uniform(math.log(m_range[0]), math.log(m_range[1])))))
+        field_type = int(rng.integers(0, 3))
+        z = float(rng.uniform(50.0, 200.0))
+        if i % 2 == 0:
+            res = float(rng.uniform(0.5, 2.0))
+            side = max(1, int(round(math.sqrt(m))))
+            span = (side - 1) * res
+            cx, cy = float(cen[0]), float(cen[1])
+            pad = 0.5 * res
+            grid = GridSpec(2, [(cx - span / 2, cx + span / 2 + pad),
+                                (cy - span / 2, cy + span / 2 + pad), (z, z)], res,
+                            (AXIS_X, AXIS_Y, AXIS_Z))
+            jobs.append(BatchJob(src, k, a, field_type, grid, side * side, 0, (), ()))
+        else:
+            half = float(rng.uniform(30.0, 120.0))
+            lo = (float(cen[0]) - half, float(cen[1]) - half, 50.0)
+            hi = (float(cen[0]) + half, float(cen[1]) + half, 200.0)
+            jobs.append(BatchJob(src, k, a, field_type, None, m, int(rng.integers(1 << 30)), lo,
+                                 hi))
+    return jobs

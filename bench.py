@@ -54,9 +54,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="grid", choices=["grid", "multipattern"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "multipattern", "batch"],
                     help="grid: the headline 256^3 field; multipattern: 1,024 patterns on "
-                         "262,144 points through the tensor-core contraction")
+                         "262,144 points through the tensor-core contraction; batch: 2,048 "
+                         "uneven jobs in one persistent launch from a CUDA graph")
     return ap.parse_args()
 
 
@@ -482,12 +483,81 @@ def run_multipattern(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ batched uneven jobs
+
+def run_batch(args):
+    """2,048 independent field jobs (249/498/996/2,490 transducers, 1e3-1e6 points, half grid
+    slices, half scatter sets) as one persistent launch replayed from a CUDA graph, against
+    the same jobs launched one by one."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    import afc
+    import batch_device as BD
+
+    lib = afc.DLL
+    lib.AFC_SetDevice(local)
+    jobs = W.batch_jobs()
+    arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    t0 = time.perf_counter()
+    plan = BD.create_plan(afc, arr, True, sh)
+    create_s = time.perf_counter() - t0
+    info = BD.describe(afc, plan)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return ts
+
+    def run_graph():
+        assert lib.AFC_BatchRun(plan, sh) == 0, afc.last_error()
+
+    def run_each():
+        assert lib.AFC_BatchRunOneByOne(plan, sh) == 0, afc.last_error()
+
+    launches0 = lib.AFC_KernelLaunchCount()
+    tb = timed(run_graph, args.steps, max(args.warmup, 1))
+    launches = (lib.AFC_KernelLaunchCount() - launches0) // (args.steps + max(args.warmup, 1))
+    te = timed(run_each, max(1, min(args.steps, 3)), 1)
+    lib.AFC_BatchFree(plan)
+    evals = info["evals"]
+    tbm, tem = statistics.median(tb), statistics.median(te)
+    line = {"metric": "source-point evaluations/s (2,048 uneven jobs, one persistent launch)",
+            "value": evals / tbm, "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tbm * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "batch_2048_uneven_jobs", "jobs": len(jobs),
+                       "evals_per_step": evals,
+                       "points_per_step": int(sum(j.n_points for j in jobs)),
+                       "autotuned": info, "plan_create_s": create_s},
+            "one_by_one": {"value": evals / tem, "ms_per_step": tem * 1e3,
+                           "launches_per_step": 2 * len(jobs)},
+            "speedup_vs_one_by_one": tem / tbm,
+            "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "multipattern":
         run_multipattern(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

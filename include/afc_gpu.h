@@ -101,6 +101,39 @@ int32_t AFC_MultiPatternDirect(int32_t source_type, const float *d_sources,
                                const float *d_phases, uint64_t patterns, float *d_out,
                                void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* ---- many independent field jobs in one persistent launch (no counterpart in the
+ * reference, which evaluates one AFC_Calculate at a time) ----
+ *
+ * A plan binds a list of jobs -- each one field evaluation of its own sources on its own grid
+ * or points into its own output -- to a CUDA graph that packs every job's sources and runs one
+ * persistent kernel over all (job, point block) work items, longest first.  The caller may
+ * rewrite the contents of the source arrays between runs; the pointers and sizes are fixed at
+ * creation.  `tune` != 0 times the candidate point tiles (1, 2, 4 point pairs per thread) on
+ * the batch and keeps the fastest.  All jobs of a plan have the same source type. */
+typedef struct AfcFieldJob {
+    uint64_t n_sources;
+    const float *d_sources; /* ABI records (AfcT4010A1 / AfcSphereWaveSource) */
+    const float *d_wavenums;
+    const float *d_attens;
+    int32_t field_type; /* 0 pressure, 1 power, 2 complex */
+    int32_t is_grid;    /* 1: `grid` gives the points; 0: d_points / n_points */
+    AfcGridDesc grid;
+    const float *d_points;
+    uint64_t n_points;
+    void *d_out;
+} AfcFieldJob;
+
+int32_t AFC_BatchCreate(int32_t source_type, const AfcFieldJob *jobs, uint64_t n_jobs,
+                        int32_t tune, void **plan, void *stream);
+/* Replays the plan's graph on `stream` (asynchronous). */
+int32_t AFC_BatchRun(void *plan, void *stream);
+/* The same jobs launched one at a time (pack + field kernel per job), for comparison. */
+int32_t AFC_BatchRunOneByOne(void *plan, void *stream);
+/* Chosen point pairs per thread, resident CTAs per SM, work items, total evaluations. */
+int32_t AFC_BatchDescribe(void *plan, int32_t *pairs, int32_t *blocks_per_sm, uint64_t *items,
+                          double *evals);
+void AFC_BatchFree(void *plan);
+
 /* Measure, on the current device, with dependency-free microbenchmarks, the result rates
  * [operations/s] of rates[0..4] = MUFU ex2, rsqrt, sqrt, sin, cos and rates[5] = FP32 FMA,
  * the SM clock [Hz] while they run, and the SM count.  These are the denominators of the

@@ -1,0 +1,112 @@
+"""Batched uneven jobs (AFC_BatchCreate / AFC_BatchRun): every job's output equals its
+one-at-a-time evaluation and the oracle, the autotuned and fixed plans agree, and source edits
+between graph replays are seen."""
+import numpy as np
+import pytest
+
+import batch_device as BD
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+@pytest.fixture(autouse=True)
+def _correctly_rounded_acos():
+    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
+        yield
+
+
+def _small_jobs():
+    jobs = W.batch_jobs(seed=21, n_jobs=10, m_range=(1.0, 4e4), counts=(249, 498))
+    # add edge cases: one point, one source, no sources
+    one = W.batch_jobs(seed=22, n_jobs=2, m_range=(1.0, 1.5), counts=(249,))
+    jobs += one
+    j = W.batch_jobs(seed=23, n_jobs=1, m_range=(300, 301), counts=(249,))[0]
+    j.sources, j.k, j.atten = j.sources[:1], j.k[:1], j.atten[:1]
+    jobs.append(j)
+    j0 = W.batch_jobs(seed=24, n_jobs=1, m_range=(100, 101), counts=(249,))[0]
+    j0.sources, j0.k, j0.atten = j0.sources[:0], j0.k[:0], j0.atten[:0]
+    jobs.append(j0)
+    return jobs
+
+
+def _points(jb, pts):
+    if jb.grid is not None:
+        lo, hi = jb.grid.lo_hi()
+        return O.grid_points(2, lo, hi, jb.grid.res, jb.grid.axes)
+    return pts.cpu().numpy()
+
+
+def _as_field(out, ft):
+    o = out.cpu().numpy()
+    return o.view(np.complex64) if ft == 2 else o
+
+
+def _oracle(jb, pts):
+    if jb.n == 0:
+        return np.zeros(len(pts), np.complex64)
+    return O.field_f32(1, jb.sources, jb.k, jb.atten, pts)
+
+
+def _check(jb, got, ref_c):
+    ft = jb.field_type
+    ref = ref_c if ft == 2 else (np.abs(ref_c) if ft == 0 else np.abs(ref_c) ** 2)
+    peak = max(float(np.max(np.abs(ref))), 1e-30)
+    assert np.max(np.abs(got - ref)) <= (2 if ft == 1 else 1) * TOL * peak
+
+
+def test_batch_matches_one_by_one_and_oracle(gpu):
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    jobs = _small_jobs()
+    arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
+    st = torch.cuda.current_stream().cuda_stream
+    for tune in (True, False):
+        plan = BD.create_plan(afc, arr, tune, st)
+        try:
+            info = BD.describe(afc, plan)
+            assert info["pairs_per_thread"] in (1, 2, 4)
+            for o in outs:
+                o.fill_(float("nan"))
+            assert afc.DLL.AFC_BatchRun(plan, st) == 0, afc.last_error()
+            torch.cuda.synchronize()
+            batched = [o.clone() for o in outs]
+            for o in outs:
+                o.fill_(float("nan"))
+            assert afc.DLL.AFC_BatchRunOneByOne(plan, st) == 0, afc.last_error()
+            torch.cuda.synchronize()
+            for jb, b, o, p in zip(jobs, batched, outs, pts):
+                a_b = _as_field(b, jb.field_type)
+                a_o = _as_field(o, jb.field_type)
+                assert np.all(np.isfinite(a_b))
+                peak = max(float(np.max(np.abs(a_o))), 1e-30) if a_o.size else 1.0
+                assert np.max(np.abs(a_b - a_o), initial=0.0) <= 1e-6 * peak
+                _check(jb, a_b, _oracle(jb, _points(jb, p)))
+        finally:
+            afc.DLL.AFC_BatchFree(plan)
+
+
+def test_batch_sees_source_edits_between_runs(gpu):
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    jobs = W.batch_jobs(seed=31, n_jobs=4, m_range=(500, 5000), counts=(249,))
+    arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
+    st = torch.cuda.current_stream().cuda_stream
+    plan = BD.create_plan(afc, arr, False, st)
+    try:
+        assert afc.DLL.AFC_BatchRun(plan, st) == 0
+        # new phases written into job 0's device source records (column 7)
+        rng = np.random.default_rng(5)
+        src_t = keep[0].view(-1, 9)
+        new_phase = rng.uniform(0, 2 * np.pi, jobs[0].n).astype(np.float32)
+        src_t[:, 7] = torch.from_numpy(new_phase).cuda()
+        jobs[0].sources[:, 7] = new_phase
+        assert afc.DLL.AFC_BatchRun(plan, st) == 0
+        torch.cuda.synchronize()
+        got = _as_field(outs[0], jobs[0].field_type)
+        _check(jobs[0], got, _oracle(jobs[0], _points(jobs[0], pts[0])))
+    finally:
+        afc.DLL.AFC_BatchFree(plan)

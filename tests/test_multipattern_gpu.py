@@ -97,3 +97,36 @@ def test_multipattern_precisions_vs_f64(gpu, K):
     assert e_bf[0] <= 1e-4
     assert e_d[0] <= 1e-4
     assert e_h[0] <= 2e-3
+
+
+def test_multipattern_full_size_sampled_rows_vs_f64(gpu):
+    """The 1,024-pattern, 262,144-point, 3,984-source contraction, checked on 128 seeded rows
+    (all patterns) against float64."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    w, amps, phases = W.multi_pattern()
+    n, m, K = w.n, len(w.points), len(amps)
+    rng = np.random.default_rng(99)
+    rows = np.sort(rng.choice(m, 128, replace=False))
+    ref = _p64(w.sources, w.k, w.atten, w.points[rows], amps, phases)
+    dev = "cuda"
+    d = [torch.from_numpy(x.reshape(-1)).to(dev)
+         for x in (w.sources, w.k, w.atten, w.points, amps, phases)]
+    st = torch.cuda.current_stream().cuda_stream
+    idx = torch.from_numpy(rows).to(dev)
+    for prec, bar in ((BF16X3, 1e-4), (FP16, 2e-3)):
+        wsb = afc.DLL.AFC_MultiPatternWorkspaceBytes(n, m, K, prec)
+        ws = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
+        base = (ws.data_ptr() + 255) // 256 * 256
+        out = torch.empty(2 * m * K, dtype=torch.float32, device=dev)
+        assert afc.DLL.AFC_MultiPatternBuildG(1, prec, d[0].data_ptr(), d[1].data_ptr(),
+                                              d[2].data_ptr(), n, d[3].data_ptr(), m, K, base,
+                                              wsb, st) == 0, afc.last_error()
+        assert afc.DLL.AFC_MultiPatternApply(prec, d[4].data_ptr(), d[5].data_ptr(), n, m, K,
+                                             out.data_ptr(), base, wsb, st) == 0, afc.last_error()
+        assert afc.DLL.AFC_MultiPatternStatus(prec, n, m, K, base, st) == 0
+        got = out.view(m, K, 2)[idx].cpu().numpy().view(np.complex64)[..., 0]
+        e = _errs(got, ref)
+        print(f"full size precision {prec}: max {e[0]:.2e} rel-L2 {e[1]:.2e}")
+        assert e[0] <= bar
+        del ws, out
