@@ -5,8 +5,8 @@ binding (python/afc/nativemethods.py:18-234) one for one, so code written agains
 drives this library unchanged.  Exports marked NEW are this library's additions (include/*.h).
 """
 import ctypes
-from ctypes import (POINTER, Structure, c_char_p, c_double, c_float, c_int, c_int32, c_size_t,
-                    c_uint, c_uint64, c_ulong, c_void_p)
+from ctypes import (POINTER, Structure, c_char_p, c_double, c_float, c_int, c_int32, c_int64,
+                    c_size_t, c_uint, c_uint64, c_ulong, c_void_p)
 
 
 class Vector3(Structure):
@@ -97,6 +97,19 @@ class FieldJob(Structure):
                 ("d_out", c_void_p)]
 
 
+class ServeConfig(Structure):
+    """NEW: AfcServeConfig of include/afc_gpu.h."""
+    _fields_ = [("hbm_budget_bytes", c_uint64), ("pinned_bytes", c_uint64),
+                ("max_inflight", c_int32)]
+
+
+class ServeStats(Structure):
+    """NEW: AfcServeStats of include/afc_gpu.h."""
+    _fields_ = [("completed", c_uint64), ("failed", c_uint64), ("queued", c_uint64),
+                ("peak_hbm_bytes", c_uint64), ("hbm_budget_bytes", c_uint64),
+                ("peak_inflight", c_int32)]
+
+
 AFC_DLL = None
 
 # Every export of include/afccapi.h and include/afc_gpu.h (checked by the symbol test).
@@ -122,7 +135,9 @@ NEW_EXPORTS = [
     "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
     "AFC_MultiPatternWorkspaceBytes", "AFC_MultiPatternBuildG", "AFC_MultiPatternApply",
     "AFC_MultiPatternStatus", "AFC_MultiPatternDirect", "AFC_BatchCreate", "AFC_BatchRun",
-    "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchFree",
+    "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchFree", "AFC_ServeCreate",
+    "AFC_ServeAddGeometry", "AFC_ServeSubmitField", "AFC_ServeSubmitGspat", "AFC_ServeWait",
+    "AFC_ServeStats", "AFC_ServeDestroy",
 ]
 
 
@@ -283,3 +298,21 @@ def __init_new():
     AFC_DLL.AFC_BatchDescribe.restype = c_int32
     AFC_DLL.AFC_BatchFree.argtypes = [c_void_p]
     AFC_DLL.AFC_BatchFree.restype = None
+    AFC_DLL.AFC_ServeCreate.argtypes = [POINTER(ServeConfig), POINTER(c_void_p)]
+    AFC_DLL.AFC_ServeCreate.restype = c_int32
+    AFC_DLL.AFC_ServeAddGeometry.argtypes = [c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                                             c_uint64, POINTER(c_int32)]
+    AFC_DLL.AFC_ServeAddGeometry.restype = c_int32
+    AFC_DLL.AFC_ServeSubmitField.argtypes = [c_void_p, c_int32, c_void_p, c_void_p, c_int32,
+                                             c_int32, POINTER(GridDesc), c_void_p, c_uint64,
+                                             c_void_p]
+    AFC_DLL.AFC_ServeSubmitField.restype = c_int64
+    AFC_DLL.AFC_ServeSubmitGspat.argtypes = [c_void_p, c_int32, c_void_p, c_void_p, c_uint64,
+                                             POINTER(GridDesc), c_void_p, c_void_p]
+    AFC_DLL.AFC_ServeSubmitGspat.restype = c_int64
+    AFC_DLL.AFC_ServeWait.argtypes = [c_void_p, c_int64, POINTER(c_double), POINTER(c_double)]
+    AFC_DLL.AFC_ServeWait.restype = c_int32
+    AFC_DLL.AFC_ServeStats.argtypes = [c_void_p, POINTER(ServeStats)]
+    AFC_DLL.AFC_ServeStats.restype = c_int32
+    AFC_DLL.AFC_ServeDestroy.argtypes = [c_void_p]
+    AFC_DLL.AFC_ServeDestroy.restype = None

@@ -55,6 +55,11 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
                          const PointSet& ps, void* out, cudaStream_t s);
 
+// Packed sources of a request: geometry from `geom`, amplitude and phase from `amps` and
+// `phases` or, when `amp_phase` is not NULL, from its interleaved (amp, phase) pairs.
+cudaError_t launch_repack(const PackedSource* geom, const float* amps, const float* phases,
+                          const float* amp_phase, int64_t n, PackedSource* out, cudaStream_t s);
+
 // Streaming multiprocessors of the current device (cached after the first query).
 int num_sms();
 

@@ -277,3 +277,50 @@ def batch_jobs(seed: int = 3, n_jobs: int = 2048, m_range=(1e3, 1e6),
             jobs.append(BatchJob(src, k, a, field_type, None, m, int(rng.integers(1 << 30)), lo,
                                  hi))
     return jobs
+
+
+def batch_job_points(job: BatchJob) -> np.ndarray:
+    """The scatter points of a scatter-set BatchJob drawn on the host from its seed
+    (float32 m x 3, uniform in the job's box)."""
+    rng = np.random.default_rng(job.points_seed)
+    lo = np.asarray(job.box_lo, np.float32)
+    hi = np.asarray(job.box_hi, np.float32)
+    return (lo + (hi - lo) * rng.random((job.n_points, 3), dtype=np.float32)).astype(np.float32)
+
+
+@dataclasses.dataclass
+class ServingRequest:
+    """One request of the serving stream: `arrival` seconds after the stream starts; a field
+    job (`job` indexes the payload pool of batch_jobs) or a GS-PAT hologram request on the
+    2 x 2 tiling (`foci`, `amps`; the slice is 201 x 201 at 1 mm over the array centre at the
+    foci's mean depth)."""
+
+    arrival: float
+    kind: str  # "field" | "gspat"
+    job: int = -1
+    foci: np.ndarray | None = None
+    amps: np.ndarray | None = None
+
+
+def serving_stream(lam: float, n_requests: int, pool_size: int, seed: int = 4,
+                   field_share: float = 0.7, foci_range=(2, 64)):
+    """A seeded Poisson stream at rate `lam` req/s: exponential inter-arrival gaps; each request
+    a field job (probability `field_share`, payload uniform over the pool) or a GS-PAT request
+    with M uniform in foci_range (inclusive), foci uniform in a 100 x 100 mm box over the 2 x 2
+    tiling's centre at z 100-200 mm, target amplitudes U[0.5, 1]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / lam, n_requests))
+    cen = array_center(tiled_array(2, 2))
+    out = []
+    for i in range(n_requests):
+        if rng.random() < field_share:
+            out.append(ServingRequest(float(t[i]), "field", job=int(rng.integers(pool_size))))
+        else:
+            m = int(rng.integers(foci_range[0], foci_range[1] + 1))
+            foci = np.empty((m, 3), np.float32)
+            foci[:, 0] = rng.uniform(cen[0] - 50, cen[0] + 50, m)
+            foci[:, 1] = rng.uniform(cen[1] - 50, cen[1] + 50, m)
+            foci[:, 2] = rng.uniform(100.0, 200.0, m)
+            amps = rng.uniform(0.5, 1.0, m).astype(np.float32)
+            out.append(ServingRequest(float(t[i]), "gspat", foci=foci, amps=amps))
+    return out

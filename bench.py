@@ -54,10 +54,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="grid", choices=["grid", "multipattern", "batch"],
+    ap.add_argument("--workload", default="grid",
+                    choices=["grid", "multipattern", "batch", "serving"],
                     help="grid: the headline 256^3 field; multipattern: 1,024 patterns on "
                          "262,144 points through the tensor-core contraction; batch: 2,048 "
-                         "uneven jobs in one persistent launch from a CUDA graph")
+                         "uneven jobs in one persistent launch from a CUDA graph; serving: a "
+                         "Poisson request stream swept over arrival rates")
+    ap.add_argument("--lams", default="100,300,1000,3000,10000",
+                    help="serving: arrival rates (req/s) of the sweep")
     return ap.parse_args()
 
 
@@ -550,6 +554,150 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ serving
+
+def run_serving(args):
+    """A seeded Poisson request stream through the serving engine (AFC_Serve*), swept over
+    arrival rates: 70% field jobs drawn from a pool of the batched-job mix (the first 256
+    jobs: 249-2,490 transducers, 1e3-1e6 points, grid slices and scatter sets), 30% GS-PAT
+    requests on the 2 x 2 tiling (M uniform in 2..64, 100 iterations, then a 201 x 201
+    pressure slice at the foci's mean depth).  Geometries are registered once and stay
+    resident; each request uploads only its drive (or foci) and points, from host memory, and
+    its result comes back to host memory.  Latency = submission to completion of the result's
+    device-to-host copy, measured by the engine."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    import afc
+    import serving_client as SC
+
+    lib = afc.DLL
+    lib.AFC_SetDevice(local)
+    pool = W.batch_jobs(n_jobs=256)
+    eng = SC.Engine(afc, hbm_budget_bytes=2 << 30, pinned_bytes=2 << 30, max_inflight=32)
+    gid_of_n = {}
+    for jb in pool:
+        if jb.n not in gid_of_n:
+            gid_of_n[jb.n] = eng.add_geometry(1, jb.sources, jb.k, jb.atten)
+    gpos = W.tiled_array(2, 2)
+    gcen = W.array_center(gpos)
+    gsrc = W.t4010a1_records(gpos, 1.0, 0.0)
+    n_g = len(gpos)
+    gid_gspat = eng.add_geometry(1, gsrc, np.full(n_g, W.wavenumber(), np.float32),
+                                 np.zeros(n_g, np.float32))
+    # per pool job: (geometry, amps, phases, field type, grid desc or None, points or None, m)
+    payload = []
+    for jb in pool:
+        amps = np.ascontiguousarray(jb.sources[:, 6])
+        phases = np.ascontiguousarray(jb.sources[:, 7])
+        if jb.grid is not None:
+            desc = afc.grid_from_spec(jb.grid).grid_desc()
+            m = int(desc.count[0] * desc.count[1] * desc.count[2])
+            payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, desc, None, m, jb.n))
+        else:
+            pts = W.batch_job_points(jb)
+            payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, None, pts,
+                            jb.n_points, jb.n))
+    slice_evals = n_g * 201 * 201
+
+    def prepare(stream):
+        out = []
+        for r in stream:
+            if r.kind == "field":
+                out.append(("field", r.arrival, payload[r.job]))
+            else:
+                desc, _ = SC.slice_desc(afc, gcen, float(r.foci[:, 2].mean()), half=100.0,
+                                        res=1.0)
+                out.append(("gspat", r.arrival, (r.foci, r.amps, desc)))
+        return out
+
+    def submit(item):
+        kind, _, p = item
+        if kind == "field":
+            gid, amps, phases, ft, desc, pts, m, n = p
+            rid, _ = eng.submit_field(gid, amps, phases, ft, grid=desc, points=pts)
+            return rid, n * m
+        foci, tamps, desc = p
+        rid, _, _ = eng.submit_gspat(gid_gspat, n_g, foci, tamps, desc)
+        return rid, slice_evals
+
+    def run_stream(items):
+        """Submit on the arrival schedule from this thread; a second thread waits."""
+        import queue as Q
+
+        q = Q.Queue()
+        lat, qwait = [], []
+        t_end = [0.0]
+
+        def waiter():
+            while True:
+                got = q.get()
+                if got is None:
+                    return
+                rid, t_sub = got
+                la, qw = eng.wait(rid)
+                lat.append(la)
+                qwait.append(qw)
+                t_end[0] = max(t_end[0], t_sub + la)
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        evals = 0
+        t0 = time.perf_counter()
+        for it in items:
+            while time.perf_counter() - t0 < it[1]:
+                pass
+            t_sub = time.perf_counter()
+            rid, ev = submit(it)
+            evals += ev
+            q.put((rid, t_sub))
+        q.put(None)
+        th.join()
+        return np.asarray(lat), np.asarray(qwait), t_end[0] - t0, evals
+
+    lams = [float(x) for x in args.lams.split(",")]
+    warm = prepare(W.serving_stream(1000.0, max(args.warmup, 1) * 20, len(pool), seed=99))
+    run_stream(warm)
+    launches0 = lib.AFC_KernelLaunchCount()
+    st0 = eng.stats()
+    sweep = []
+    for i, lam in enumerate(lams):
+        n_req = int(min(max(lam * 2.0, 200), 5000))
+        items = prepare(W.serving_stream(lam, n_req, len(pool), seed=4 + i))
+        lat, qw, span, evals = run_stream(items)
+        sweep.append({"offered_req_s": lam, "requests": n_req,
+                      "gspat_requests": sum(1 for it in items if it[0] == "gspat"),
+                      "achieved_req_s": n_req / span, "span_s": span,
+                      "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                      "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                      "queue_p50_ms": float(np.percentile(qw, 50) * 1e3),
+                      "queue_p99_ms": float(np.percentile(qw, 99) * 1e3),
+                      "field_evals_per_s": evals / span})
+    launches = lib.AFC_KernelLaunchCount() - launches0
+    st = eng.stats()
+    eng.close()
+    best = max(sweep, key=lambda s: s["achieved_req_s"])
+    line = {"metric": "requests/s (serving: Poisson stream, 70% field jobs / 30% GS-PAT)",
+            "value": best["achieved_req_s"], "unit": "req/s", "n_gpus": 1,
+            "steps": len(lams), "warmup": max(args.warmup, 1),
+            "ms_per_step": best["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "serving_poisson_field70_gspat30", "pool_jobs": len(pool),
+                       "gspat_sources": n_g, "gspat_foci": [2, 64], "gspat_iterations": 100,
+                       "slice": [201, 201], "hbm_budget_bytes": st["hbm_budget_bytes"],
+                       "max_inflight": 32},
+            "sweep": sweep,
+            "engine": {"completed": st["completed"] - st0["completed"], "failed": st["failed"],
+                       "peak_inflight": st["peak_inflight"],
+                       "peak_hbm_bytes": st["peak_hbm_bytes"]},
+            "e2e": {"value": best["achieved_req_s"], "unit": "req/s",
+                    "note": "host buffers in and out; every request's copies are inside its "
+                            "latency"},
+            "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -558,6 +706,8 @@ def main():
         run_multipattern(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

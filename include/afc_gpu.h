@@ -134,6 +134,53 @@ int32_t AFC_BatchDescribe(void *plan, int32_t *pairs, int32_t *blocks_per_sm, ui
                           double *evals);
 void AFC_BatchFree(void *plan);
 
+/* ---- serving engine (no counterpart in the reference, whose calls block) ----
+ *
+ * Field-evaluation and GS-PAT hologram requests on resident geometries, admitted in arrival
+ * order under a fixed HBM budget (a device arena of hbm_budget_bytes) and at most
+ * max_inflight at a time, each on its own stream so that admitted requests overlap on the GPU
+ * while later ones keep arriving.  Inputs are copied at submission (into a pinned host arena of
+ * pinned_bytes; submission waits while it is full); results land in the caller's buffers before
+ * AFC_ServeWait returns.  Latency is measured from submission until the request's last
+ * device operation (the copy of its result to host memory) has completed. */
+typedef struct AfcServeConfig {
+    uint64_t hbm_budget_bytes;
+    uint64_t pinned_bytes;
+    int32_t max_inflight;
+} AfcServeConfig;
+
+typedef struct AfcServeStats {
+    uint64_t completed;
+    uint64_t failed;
+    uint64_t queued;
+    uint64_t peak_hbm_bytes;
+    uint64_t hbm_budget_bytes;
+    int32_t peak_inflight;
+} AfcServeStats;
+
+int32_t AFC_ServeCreate(const AfcServeConfig *config, void **engine);
+/* Register sources (ABI records, wavenumbers, attenuations): packed once, resident. */
+int32_t AFC_ServeAddGeometry(void *engine, int32_t source_type, const float *h_sources,
+                             const float *h_wavenums, const float *h_attens, uint64_t n,
+                             int32_t *geometry_id);
+/* Field of the geometry with these amplitudes and phases on a grid (is_grid) or on n_points
+ * explicit points; h_out receives floats (pressure, power) or float pairs (complex).
+ * Returns the request id (> 0) or a negative AFC_ERR_* code. */
+int64_t AFC_ServeSubmitField(void *engine, int32_t geometry, const float *h_amps,
+                             const float *h_phases, int32_t field_type, int32_t is_grid,
+                             const AfcGridDesc *grid, const float *h_points, uint64_t n_points,
+                             float *h_out);
+/* GS-PAT on the geometry (amplitudes as registered) for n_foci foci, then the pressure of
+ * the solved drive on `slice`; h_amp_phase_out (optional) receives the drive (amp, phase). */
+int64_t AFC_ServeSubmitGspat(void *engine, int32_t geometry, const float *h_foci,
+                             const float *h_amps, uint64_t n_foci, const AfcGridDesc *slice,
+                             float *h_slice_out, float *h_amp_phase_out);
+/* Blocks until the request has finished; its latency and time spent queued [s]. */
+int32_t AFC_ServeWait(void *engine, int64_t request, double *latency_s, double *queue_s);
+int32_t AFC_ServeStats(void *engine, AfcServeStats *stats);
+/* Finishes queued and running requests, then frees the engine. */
+void AFC_ServeDestroy(void *engine);
+
 /* Measure, on the current device, with dependency-free microbenchmarks, the result rates
  * [operations/s] of rates[0..4] = MUFU ex2, rsqrt, sqrt, sin, cos and rates[5] = FP32 FMA,
  * the SM clock [Hz] while they run, and the SM count.  These are the denominators of the
