@@ -105,9 +105,10 @@ __device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase
 }
 
 // Correction for one point whose fast theta fell next to a bin edge: recompute the pair with
-// the same fast operations (UD: cos(theta) from the shared direction) and return
-// w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators.  Everything
-// passes by value so that the caller's accumulators stay in registers.
+// the same fast operations (UD: cos(theta) from the shared direction), find the reference's
+// bin (exact_bin) and, where it differs from the fast one, return w (D_exact - D_fast)
+// (cos, sin), the amount to add to the point's accumulators.  Everything passes by value so
+// that the caller's accumulators stay in registers.
 template <bool UD>
 __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
                                                float4 v2, float4 v3, float4 v4, float2 ns,
@@ -115,8 +116,6 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
     const float dx = px + v0.x, dy = py + v0.z, dz = pz + v1.x;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float rinv = mufu_rsqrt(r2);
-    const float r = r2 * rinv;
-    const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
     float ct, nx, ny, nz;
     if constexpr (UD) {
         ct = (np + ns.x) * rinv;
@@ -129,11 +128,14 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
         ny = v2.z;
         nz = v3.x;
     }
-    unsigned near;
-    const float d_fast = directivity2_fast(tab, make_float2(ct, ct), near).x;
-    const float d_exact = directivity_exact(tab, dx, dy, dz, nx, ny, nz);
+    const float th = acos2_fast(make_float2(ct, ct)).x;
+    const int i_fast = fast_bin(th);
+    const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
+    if (i_exact == i_fast) return make_float2(0.f, 0.f);
+    const float r = r2 * rinv;
+    const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
     const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
-    const float corr = w0 * (d_exact - d_fast);
+    const float corr = w0 * (dir_in_bin(tab, th, i_exact) - dir_in_bin(tab, th, i_fast));
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 

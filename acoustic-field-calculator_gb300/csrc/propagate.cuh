@@ -14,8 +14,11 @@
 // degrees (by 0.016, 0.003, 0.047 and 0.164).  A theta within rounding of a bin edge can land
 // in a different bin than the reference's f32 arithmetic puts it, which changes that pair's
 // term by up to 16 %.  Pairs whose fast theta lies within kEdgeMargin of an edge therefore take
-// directivity_exact(), which repeats the reference's f32 operations (no FMA, IEEE sqrt and
-// division, acos correctly rounded from double) so that the bin is the reference's.
+// the exact bin: cos(theta) by the reference's f32 operations (no FMA, IEEE sqrt and division),
+// then compared with the ten float thresholds kBinCos1..10 at which the reference's bin
+// ceil(acos(c) / ANGLE_DIV) -- acos correctly rounded to f32 -- steps (derived and checked
+// exhaustively around every edge in bin_edges.py).  The cubic of that bin is evaluated at the
+// fast theta (within 3e-6 rad).  No double-precision operation is involved.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,6 +49,19 @@ constexpr float kInvAngleDiv = 18.0f / 3.14159265358979323846f;
 // rounding in cos(theta)), so 1e-5 leaves a factor of three.
 constexpr float kEdgeMargin = 1.0e-5f;
 constexpr float kEdgeBound = 0.5f * kAngleDiv - kEdgeMargin;
+
+// bin(c) = #{b : c <= kBinCos_b} reproduces the reference's bin (0..10, NaN -> 0) for every
+// float c = cos(theta) (bin_edges.py).
+constexpr float kBinCos1 = 0x1.fffffep-1f;    // 0.99999994
+constexpr float kBinCos2 = 0x1.f838b8p-1f;    // 0.98480773
+constexpr float kBinCos3 = 0x1.e11f62p-1f;    // 0.939692557
+constexpr float kBinCos4 = 0x1.bb67acp-1f;    // 0.866025329
+constexpr float kBinCos5 = 0x1.8836f8p-1f;    // 0.766044378
+constexpr float kBinCos6 = 0x1.491b72p-1f;    // 0.642787516
+constexpr float kBinCos7 = 0x1.fffffap-2f;    // 0.499999911
+constexpr float kBinCos8 = 0x1.5e3a82p-2f;    // 0.342020065
+constexpr float kBinCos9 = 0x1.63a194p-3f;    // 0.17364803
+constexpr float kBinCos10 = -0x1.ddde98p-23f;  // -2.2252533e-07
 
 // acos(c) = sqrt(1 - c) * Q(c); Q of degree 5 fitted in fit_acos.py (float32 error <= 1.7e-6
 // rad on [-0.03, 1]; for c in [-1, -0.02] it stays between 1.59 and 2.75 rad, i.e. beyond 90
@@ -111,23 +127,18 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 
 // ------------------------------------------------------------------ directivity
 
-// The reference's own f32 arithmetic for theta and its bin (uniform_medium.rs:113-116,
-// t4010a1.rs:107-120): |d| = sqrt((dx dx + dy dy) + dz dz), cos = ((nx dx + ny dy) + nz dz) / |d|,
-// theta = acos(cos) rounded to f32, i = ceil(theta / ANGLE_DIV).
-static __device__ __noinline__ float directivity_exact(const float4* __restrict__ tab, float dx,
-                                                float dy, float dz, float nx, float ny, float nz) {
+// The reference's bin for one pair (uniform_medium.rs:113-116, t4010a1.rs:107-120): its f32
+// cos(theta) = ((nx dx + ny dy) + nz dz) / sqrt((dx dx + dy dy) + dz dz) without contraction,
+// IEEE sqrt and division, then the threshold count.
+static __device__ __noinline__ int exact_bin(float dx, float dy, float dz, float nx, float ny,
+                                             float nz) {
     const float dist = __fsqrt_rn(
         __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
     const float dot = __fadd_rn(__fadd_rn(__fmul_rn(nx, dx), __fmul_rn(ny, dy)), __fmul_rn(nz, dz));
-    const float ct = __fdiv_rn(dot, dist);
-    const float theta = __double2float_rn(acos(static_cast<double>(ct)));
-    const float q = ceilf(__fdiv_rn(theta, kAngleDiv));
-    if (!(q > 0.0f)) return 1.0f;  // bin 0, and NaN (`as usize` gives 0)
-    if (q > 9.0f) return 0.0f;
-    const int i = static_cast<int>(q);
-    const float4 c = tab[i];
-    const float x = __fsub_rn(theta, __fmul_rn(__fsub_rn(static_cast<float>(i), 1.0f), kAngleDiv));
-    return __fadd_rn(c.x, __fmul_rn(__fadd_rn(c.y, __fmul_rn(__fadd_rn(c.z, __fmul_rn(c.w, x)), x)), x));
+    const float c = __fdiv_rn(dot, dist);
+    return (c <= kBinCos1) + (c <= kBinCos2) + (c <= kBinCos3) + (c <= kBinCos4) +
+           (c <= kBinCos5) + (c <= kBinCos6) + (c <= kBinCos7) + (c <= kBinCos8) +
+           (c <= kBinCos9) + (c <= kBinCos10);
 }
 
 // Fast theta from cos(theta) for two points.
@@ -145,6 +156,28 @@ __device__ __forceinline__ float2 acos2_fast(float2 ct) {
     return mul2(s, q);
 }
 
+// The bin the fast path takes for theta th: ceil(th / ANGLE_DIV) clipped to 10 (the packed
+// form is in directivity2_fast).
+__device__ __forceinline__ int fast_bin(float th) {
+    const unsigned i =
+        static_cast<unsigned>(__float_as_int(__fmaf_ru(th, kInvAngleDiv, kTwo23)) - kTwo23Bits);
+    return static_cast<int>(min(i, 10u));
+}
+
+// The cubic of bin i (0..10) at theta th.
+__device__ __forceinline__ float dir_in_bin(const float4* __restrict__ tab, float th, int i) {
+    const float4 c = tab[i];
+    const float x = fmaf(static_cast<float>(i - 1), -kAngleDiv, th);
+    return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
+}
+
+// Directivity of one pair whose fast theta th fell next to a bin edge: the exact bin's cubic.
+__device__ __forceinline__ float directivity_exact(const float4* __restrict__ tab, float th,
+                                                   float dx, float dy, float dz, float nx,
+                                                   float ny, float nz) {
+    return dir_in_bin(tab, th, exact_bin(dx, dy, dz, nx, ny, nz));
+}
+
 // Bin lookup and cubic for one point given its fast theta and 2^23 + ceil(theta / ANGLE_DIV)
 // computed in packed form by the caller: returns D and whether theta lies within kEdgeMargin
 // of a bin edge (testing every edge costs fewer instructions than selecting the four where
@@ -160,7 +193,7 @@ __device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float
 
 // Fast directivity of two points (packed) from their cos(theta); `near` receives, in bits 0
 // and 1, whether each point's theta lies within kEdgeMargin of a bin edge (the caller then
-// replaces that point's term through directivity_exact).
+// replaces that point's directivity by the exact bin's).
 __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ tab, float2 ct,
                                                     unsigned& near) {
     const float2 th = acos2_fast(ct);
@@ -181,8 +214,11 @@ __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, f
                                                float2 dy, float2 dz, float nx, float ny, float nz) {
     unsigned near;
     float2 d = directivity2_fast(tab, ct, near);
-    if (near & 1u) d.x = directivity_exact(tab, dx.x, dy.x, dz.x, nx, ny, nz);
-    if (near & 2u) d.y = directivity_exact(tab, dx.y, dy.y, dz.y, nx, ny, nz);
+    if (near) {
+        const float2 th = acos2_fast(ct);
+        if (near & 1u) d.x = directivity_exact(tab, th.x, dx.x, dy.x, dz.x, nx, ny, nz);
+        if (near & 2u) d.y = directivity_exact(tab, th.y, dx.y, dy.y, dz.y, nx, ny, nz);
+    }
     return d;
 }
 

@@ -62,6 +62,11 @@ def parse():
                          "Poisson request stream swept over arrival rates")
     ap.add_argument("--lams", default="100,300,1000,3000,10000",
                     help="serving: arrival rates (req/s) of the sweep")
+    # smaller cases of the same kernels (profiling); the defaults are the workloads above
+    ap.add_argument("--grid-count", type=int, default=256, help="grid: points per axis")
+    ap.add_argument("--mp-points", type=int, default=262144, help="multipattern: points")
+    ap.add_argument("--mp-patterns", type=int, default=1024, help="multipattern: patterns")
+    ap.add_argument("--batch-jobs", type=int, default=2048, help="batch: job count")
     return ap.parse_args()
 
 
@@ -72,9 +77,9 @@ def dist_env():
     return rank, world, local
 
 
-def config_dict(w, extra=None):
-    d = {"workload": w.name, "sources": w.n, "grid": [256, 256, 256], "resolution_mm": 0.5,
-         "points": 256 ** 3, "evals_per_step": w.n * 256 ** 3, "field": "complex pressure",
+def config_dict(w, count, extra=None):
+    d = {"workload": w.name, "sources": w.n, "grid": [count] * 3, "resolution_mm": 0.5,
+         "points": count ** 3, "evals_per_step": w.n * count ** 3, "field": "complex pressure",
          "attenuation_per_mm": 1.15e-2, "seed": 1, "parallelism": "replicas (no collective)"}
     if extra:
         d.update(extra)
@@ -145,7 +150,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "impl": "reference",
-            "config": config_dict(w, {"sample_points_per_step": len(pts)}),
+            "config": config_dict(w, 256, {"sample_points_per_step": len(pts)}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"each step: 1 z-plane of the grid ({len(pts)} points x "
                                        f"{w.n} sources = {evals:.3e} evals); the reference is "
@@ -249,8 +254,9 @@ def run_ours(args):
     lib = afc.DLL
     if lib.AFC_SetDevice(local) != 0:
         raise RuntimeError(afc.last_error())
-    w = W.large_grid()
-    evals = w.n * 256 ** 3
+    count = args.grid_count
+    w = W.large_grid(count=count)
+    evals = w.n * count ** 3
 
     # ---- device-resident arm (value)
     system = afc.UniformSystem(300.0)
@@ -258,7 +264,7 @@ def run_ours(args):
     area = afc.grid_from_spec(w.grid)
     desc = area.grid_desc()
     m = int(desc.count[0] * desc.count[1] * desc.count[2])
-    assert m == 256 ** 3
+    assert m == count ** 3
     dev = torch.device("cuda", local)
     d_src = torch.from_numpy(w.sources.reshape(-1)).to(dev)
     d_k = torch.from_numpy(w.k).to(dev)
@@ -358,7 +364,7 @@ def run_ours(args):
             "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": config_dict(w, {"l2": "flushed between timed steps (256 MiB write)"}),
+            "config": config_dict(w, count, {"l2": "flushed between timed steps (256 MiB write)"}),
             "e2e": {"value": evals * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                     "api": "AFC_Calculate (reference C ABI), host buffers"},
@@ -391,7 +397,7 @@ def run_multipattern(args):
 
     lib = afc.DLL
     lib.AFC_SetDevice(local)
-    w, amps, phases = W.multi_pattern()
+    w, amps, phases = W.multi_pattern(m=args.mp_points, patterns=args.mp_patterns)
     n, m, K = w.n, len(w.points), len(amps)
     evals = n * m * K
     dev = torch.device("cuda", local)
@@ -502,7 +508,7 @@ def run_batch(args):
 
     lib = afc.DLL
     lib.AFC_SetDevice(local)
-    jobs = W.batch_jobs()
+    jobs = W.batch_jobs(n_jobs=args.batch_jobs)
     arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
@@ -543,7 +549,7 @@ def run_batch(args):
             "value": evals / tbm, "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tbm * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "batch_2048_uneven_jobs", "jobs": len(jobs),
+            "config": {"workload": f"batch_{len(jobs)}_uneven_jobs", "jobs": len(jobs),
                        "evals_per_step": evals,
                        "points_per_step": int(sum(j.n_points for j in jobs)),
                        "autotuned": info, "plan_create_s": create_s},

@@ -115,6 +115,13 @@ ORC_EXPORT void oracle_wavenum_atten(float temperature, float freq, float *k, fl
 
 /* ---------------------------------------------------------------- directivity */
 
+/* The bin index of t4010a1.rs:107-120: ceil(theta / ANGLE_DIV) as usize (NaN -> 0), clipped
+ * to 10 (every index above 9 evaluates to 0). */
+ORC_EXPORT int oracle_directivity_bin(float theta) {
+    size_t i = rust_f32_as_usize(ceilf(theta / ANGLE_DIV_F));
+    return i > 10 ? 10 : (int)i;
+}
+
 /* t4010a1.rs:107-120 in f32. */
 ORC_EXPORT float oracle_directivity_t4010a1(float theta) {
     size_t i = rust_f32_as_usize(ceilf(theta / ANGLE_DIV_F));
@@ -151,6 +158,15 @@ ORC_EXPORT void oracle_set_acos_mode(int mode) { g_acos_mode = mode; }
 
 static inline float ref_acosf(float c) {
     return g_acos_mode ? (float)acos((double)c) : acosf(c);
+}
+
+/* theta = acos(c) as the reference computes it (libm or correctly rounded, see
+ * oracle_set_acos_mode). */
+ORC_EXPORT float oracle_theta_of_cos(float c) { return ref_acosf(c); }
+
+/* out[i] = the directivity bin of theta = acos(c[i]) (t4010a1.rs:107-120; clipped to 10). */
+ORC_EXPORT void oracle_bins_of_cos(const float *c, int64_t n, int *out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = oracle_directivity_bin(ref_acosf(c[i]));
 }
 
 /* ---------------------------------------------------------------- propagate */

@@ -49,6 +49,11 @@ def lib() -> ctypes.CDLL:
         L.oracle_directivity_t4010a1.restype = c_float
         L.oracle_directivity_t4010a1_f64.argtypes = [c_double]
         L.oracle_directivity_t4010a1_f64.restype = c_double
+        L.oracle_directivity_bin.argtypes = [c_float]
+        L.oracle_directivity_bin.restype = c_int
+        L.oracle_theta_of_cos.argtypes = [c_float]
+        L.oracle_theta_of_cos.restype = c_float
+        L.oracle_bins_of_cos.argtypes = [fp, c_int64, POINTER(c_int)]
         L.oracle_propagate.argtypes = [c_int, fp, c_float, c_float, c_float, c_float, c_float, fp]
         L.oracle_field_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, c_int, fp, c_int]
         L.oracle_field_accurate_f32.argtypes = L.oracle_field_f32.argtypes
@@ -123,6 +128,24 @@ def directivity(theta: float) -> float:
 
 def directivity_f64(theta: float) -> float:
     return float(lib().oracle_directivity_t4010a1_f64(theta))
+
+
+def directivity_bin(theta: float) -> int:
+    """The reference's bin index for theta (NaN -> 0, clipped to 10)."""
+    return int(lib().oracle_directivity_bin(theta))
+
+
+def theta_of_cos(c: float) -> float:
+    """acos(c) in f32 as the reference computes it (per the acos mode)."""
+    return float(lib().oracle_theta_of_cos(c))
+
+
+def bins_of_cos(c) -> np.ndarray:
+    """The reference's directivity bin of acos(c) for each float32 c (per the acos mode)."""
+    c = np.ascontiguousarray(c, dtype=np.float32)
+    out = np.empty(len(c), dtype=np.int32)
+    lib().oracle_bins_of_cos(_f(c), len(c), out.ctypes.data_as(POINTER(c_int)))
+    return out
 
 
 def _src_args(st, sources, k, atten):
