@@ -94,6 +94,7 @@ __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); 
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
 __device__ __forceinline__ float& lane_of(float2& v, int hi) { return hi ? v.y : v.x; }
+__device__ __forceinline__ float lane_of(const float2& v, int hi) { return hi ? v.y : v.x; }
 
 // Reduced phase phi + k r - n 2pi in [-pi, pi] for two points, with 2 pi rounded to f32:
 // the reduction error n (2 pi - float(2 pi)) is below 1.2e-5 rad for n < 70 turns (distances
@@ -104,11 +105,11 @@ __device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase
     return fma2(nq, f2(-kTwoPiHi), ph);
 }
 
-// Correction for one point whose fast theta fell next to a bin edge: recompute the pair with
-// the same fast operations (UD: cos(theta) from the shared direction), find the reference's
-// bin (exact_bin) and, where it differs from the fast one, return w (D_exact - D_fast)
-// (cos, sin), the amount to add to the point's accumulators.  Everything passes by value so
-// that the caller's accumulators stay in registers.
+// Correction for one point of a thread whose points include one next to a bin edge: recompute
+// the pair with the hot loop's operations (UD: cos(theta) from the shared direction); if its
+// fast theta is next to an edge and the reference's bin (exact_bin) differs from the fast one,
+// return w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators, else
+// zero.  Everything passes by value so that the caller's accumulators stay in registers.
 template <bool UD>
 __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
                                                float4 v2, float4 v3, float4 v4, float2 ns,
@@ -128,6 +129,9 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
         ny = v2.z;
         nz = v3.x;
     }
+    float2 xc;
+    directivity2_fast(tab, make_float2(ct, ct), xc);
+    if (!near_edge(xc.x)) return make_float2(0.f, 0.f);
     const float th = acos2_fast(make_float2(ct, ct)).x;
     const int i_fast = fast_bin(th);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
@@ -139,7 +143,26 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 
-// The PAIRS point pairs of one thread against shared-memory source j.
+// The geometry of point pair q against source (v0, v1, v2, v3, ns): d, r^2, 1/r, cos(theta),
+// with the same operations on the hot loop and on its edge path.
+template <bool UD>
+struct PairGeom {
+    float2 dx, dy, dz, r2, rinv, ct;
+    __device__ __forceinline__ PairGeom(float2 px, float2 py, float2 pz, float2 np, float4 v0,
+                                        float4 v1, float4 v2, float4 v3, float2 ns) {
+        dx = add2(px, lo2(v0));
+        dy = add2(py, hi2(v0));
+        dz = add2(pz, lo2(v1));
+        r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        rinv = make_float2(mufu_rsqrt(r2.x), mufu_rsqrt(r2.y));
+        if constexpr (UD) ct = mul2(add2(np, ns), rinv);
+        else ct = mul2(fma2(lo2(v3), dz, fma2(hi2(v2), dy, mul2(lo2(v2), dx))), rinv);
+    }
+};
+
+// The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
+// records whether any of the thread's points has its theta next to a bin edge; that rare case
+// recomputes the pairs' geometry to find which points, and corrects them one by one.
 template <int ST, int SUM, int PAIRS, bool UD>
 __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, float3 n0,
                                                   float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
@@ -153,24 +176,17 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         if constexpr (UD) ns = sm.ns[j];
         else v2 = sm.v2[j];
     }
-    unsigned near_mask = 0;
+    bool any_near = false;
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
-        const float2 dx = add2(PX[q], lo2(v0));
-        const float2 dy = add2(PY[q], hi2(v0));
-        const float2 dz = add2(PZ[q], lo2(v1));
-        const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        const float2 rinv = make_float2(mufu_rsqrt(r2.x), mufu_rsqrt(r2.y));
-        const float2 r = mul2(r2, rinv);
+        const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
+        const float2 r = mul2(p.r2, p.rinv);
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
-        float2 w = mul2(rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
+        float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
-            float2 ct;
-            if constexpr (UD) ct = mul2(add2(NP[q], ns), rinv);
-            else ct = mul2(fma2(lo2(v3), dz, fma2(hi2(v2), dy, mul2(lo2(v2), dx))), rinv);
-            unsigned near;
-            w = mul2(w, directivity2_fast(sm.dir, ct, near));
-            near_mask |= near << (2 * q);
+            float2 xc;
+            w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
+            any_near |= near_edge(xc.x) | near_edge(xc.y);
         }
         const float2 red = reduce_phase2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -187,21 +203,19 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         }
     }
     if constexpr (ST == SRC_T4010A1) {
-        if (near_mask) {
+        if (any_near) {
 #pragma unroll
             for (int k = 0; k < 2 * PAIRS; ++k) {
-                if (near_mask & (1u << k)) {
-                    const int q = k >> 1, h = k & 1;
-                    const float2 c = edge_correction<UD>(sm.dir, v0, v1, v2, v3, v4, ns, n0,
-                                                         lane_of(NP[q], h), lane_of(PX[q], h),
-                                                         lane_of(PY[q], h), lane_of(PZ[q], h));
-                    if constexpr (SUM == SUM_PLAIN) {
-                        lane_of(RE[q], h) += c.x;
-                        lane_of(IM[q], h) += c.y;
-                    } else {
-                        neumaier_add(lane_of(RE[q], h), lane_of(CRE[q], h), c.x);
-                        neumaier_add(lane_of(IM[q], h), lane_of(CIM[q], h), c.y);
-                    }
+                const int q = k >> 1, h = k & 1;
+                const float2 c = edge_correction<UD>(sm.dir, v0, v1, v2, v3, v4, ns, n0,
+                                                     lane_of(NP[q], h), lane_of(PX[q], h),
+                                                     lane_of(PY[q], h), lane_of(PZ[q], h));
+                if constexpr (SUM == SUM_PLAIN) {
+                    lane_of(RE[q], h) += c.x;
+                    lane_of(IM[q], h) += c.y;
+                } else {
+                    neumaier_add(lane_of(RE[q], h), lane_of(CRE[q], h), c.x);
+                    neumaier_add(lane_of(IM[q], h), lane_of(CIM[q], h), c.y);
                 }
             }
         }

@@ -75,7 +75,8 @@ constexpr float kAcos5 = -0.0045999325811862946f;
 
 // T4010A1 directivity coefficients (t4010a1.rs:18-69) as (a, b, c, d) per bin.  Entry 0
 // (theta == 0) evaluates to 1 like the reference's `0 => 1.0` arm, entries 1 and 2 are the
-// constant-1 bins, and entry 10 stands for every bin above 9, which evaluates to 0.
+// constant-1 bins, and entry 10 (with the zero-filled entries after it) stands for every bin
+// above 9, which evaluates to 0.
 #define AFC_DIR_TABLE_INIT                                                                      \
     {                                                                                           \
         {1.0f, 0.f, 0.f, 0.f}, {1.0f, 0.f, 0.f, 0.f}, {1.0f, 0.f, 0.f, 0.f},                    \
@@ -88,7 +89,9 @@ constexpr float kAcos5 = -0.0045999325811862946f;
             {0.199526231f, -0.179254124486545f, 0.008242027161100222f, -0.9016569137759131f},   \
             {0.f, 0.f, 0.f, 0.f},                                                               \
     }
-constexpr int kDirTableSize = 11;
+// The fast path indexes the table with the low five bits of 2^23 + ceil(theta / ANGLE_DIV)
+// (theta < 2.8 rad, so ceil(...) <= 16): entries 10..31 are zero like entry 10.
+constexpr int kDirTableSize = 32;
 
 // ------------------------------------------------------------------ MUFU operations
 
@@ -141,13 +144,12 @@ static __device__ __noinline__ int exact_bin(float dx, float dy, float dz, float
            (c <= kBinCos9) + (c <= kBinCos10);
 }
 
-// Fast theta from cos(theta) for two points.
+// Fast theta from cos(theta) for two points.  A c rounded above 1 gives sqrt(|1 - c|), a theta
+// of a few 1e-4 rad at most: bin 1, where the directivity is 1 as at theta = 0.
 __device__ __forceinline__ float2 acos2_fast(float2 ct) {
     const float2 c = ct;
-    float2 om = fma2(c, f2(-1.0f), f2(1.0f));  // 1 - c
-    om.x = fmaxf(om.x, 0.0f);                  // c rounded above 1 -> theta 0
-    om.y = fmaxf(om.y, 0.0f);
-    const float2 s = make_float2(mufu_sqrt(om.x), mufu_sqrt(om.y));
+    const float2 om = fma2(c, f2(-1.0f), f2(1.0f));  // 1 - c
+    const float2 s = make_float2(mufu_sqrt(fabsf(om.x)), mufu_sqrt(fabsf(om.y)));
     float2 q = fma2(f2(kAcos5), c, f2(kAcos4));
     q = fma2(q, c, f2(kAcos3));
     q = fma2(q, c, f2(kAcos2));
@@ -156,12 +158,11 @@ __device__ __forceinline__ float2 acos2_fast(float2 ct) {
     return mul2(s, q);
 }
 
-// The bin the fast path takes for theta th: ceil(th / ANGLE_DIV) clipped to 10 (the packed
-// form is in directivity2_fast).
+// The bin the fast path takes for theta th, ceil(th / ANGLE_DIV), clipped to 10 (the packed
+// form is in directivity2_fast; bins 10 and above all evaluate to 0).
 __device__ __forceinline__ int fast_bin(float th) {
-    const unsigned i =
-        static_cast<unsigned>(__float_as_int(__fmaf_ru(th, kInvAngleDiv, kTwo23)) - kTwo23Bits);
-    return static_cast<int>(min(i, 10u));
+    const int i = __float_as_int(__fmaf_ru(th, kInvAngleDiv, kTwo23)) & (kDirTableSize - 1);
+    return i < 10 ? i : 10;
 }
 
 // The cubic of bin i (0..10) at theta th.
@@ -178,46 +179,42 @@ __device__ __forceinline__ float directivity_exact(const float4* __restrict__ ta
     return dir_in_bin(tab, th, exact_bin(dx, dy, dz, nx, ny, nz));
 }
 
-// Bin lookup and cubic for one point given its fast theta and 2^23 + ceil(theta / ANGLE_DIV)
-// computed in packed form by the caller: returns D and whether theta lies within kEdgeMargin
-// of a bin edge (testing every edge costs fewer instructions than selecting the four where
-// the directivity jumps, and the exact path returns the same D at the others).
+// Bin lookup and cubic for one point given 2^23 + ceil(theta / ANGLE_DIV) (whose low five bits
+// are the bin) and x = theta - (bin - 1) ANGLE_DIV.
 __device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float fq_biased,
-                                           float x, bool& near_edge) {
-    unsigned i = static_cast<unsigned>(__float_as_int(fq_biased) - kTwo23Bits);
-    i = min(i, 10u);  // theta beyond 90 degrees, or anything unexpected, reads the zero entry
-    const float4 c = tab[i];
-    near_edge = fabsf(x - 0.5f * kAngleDiv) > kEdgeBound;
+                                           float x) {
+    const float4 c = tab[__float_as_int(fq_biased) & (kDirTableSize - 1)];
     return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
 }
 
-// Fast directivity of two points (packed) from their cos(theta); `near` receives, in bits 0
-// and 1, whether each point's theta lies within kEdgeMargin of a bin edge (the caller then
-// replaces that point's directivity by the exact bin's).
+// Fast directivity of two points (packed) from their cos(theta).  `xc` receives each point's
+// offset from the centre of its bin: |xc| > kEdgeBound marks a theta within kEdgeMargin of a
+// bin edge, where the caller replaces the directivity by the exact bin's (testing every edge
+// costs fewer instructions than selecting the four where the directivity jumps, and the exact
+// bin gives the same D at the others).
 __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ tab, float2 ct,
-                                                    unsigned& near) {
+                                                    float2& xc) {
     const float2 th = acos2_fast(ct);
     const float2 fq = __ffma2_ru(th, f2(kInvAngleDiv), f2(kTwo23));     // 2^23 + ceil(q)
     const float2 fi = add2(fq, f2(-kTwo23));                             // ceil(q)
     const float2 x = fma2(fi, f2(-kAngleDiv), add2(th, f2(kAngleDiv)));  // th - (fi-1) div
-    bool ex, ey;
-    float2 d;
-    d.x = dir_cubic(tab, fq.x, x.x, ex);
-    d.y = dir_cubic(tab, fq.y, x.y, ey);
-    near = (ex ? 1u : 0u) | (ey ? 2u : 0u);
-    return d;
+    xc = add2(x, f2(-0.5f * kAngleDiv));
+    return make_float2(dir_cubic(tab, fq.x, x.x), dir_cubic(tab, fq.y, x.y));
 }
+
+__device__ __forceinline__ bool near_edge(float xc) { return fabsf(xc) > kEdgeBound; }
 
 // Directivity of two points with the exact path applied in place (used where the pair is not
 // on the hot loop).
 __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, float2 ct, float2 dx,
                                                float2 dy, float2 dz, float nx, float ny, float nz) {
-    unsigned near;
-    float2 d = directivity2_fast(tab, ct, near);
-    if (near) {
+    float2 xc;
+    float2 d = directivity2_fast(tab, ct, xc);
+    const bool ex = near_edge(xc.x), ey = near_edge(xc.y);
+    if (ex | ey) {
         const float2 th = acos2_fast(ct);
-        if (near & 1u) d.x = directivity_exact(tab, th.x, dx.x, dy.x, dz.x, nx, ny, nz);
-        if (near & 2u) d.y = directivity_exact(tab, th.y, dx.y, dy.y, dz.y, nx, ny, nz);
+        if (ex) d.x = directivity_exact(tab, th.x, dx.x, dy.x, dz.x, nx, ny, nz);
+        if (ey) d.y = directivity_exact(tab, th.y, dx.y, dy.y, dz.y, nx, ny, nz);
     }
     return d;
 }
