@@ -45,6 +45,10 @@ UNIT = "evals/s"
 # MUFU pipe; 32 FP32-pipe operations)
 MUFU_PER_EVAL = 5
 FP32_PER_EVAL = 32
+# DRAM bytes (read + write) of one 256^3 launch of the field kernel, from an ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum (3.96 MB + 77.82 MB; part of the 134 MB output
+# is still in L2 when the launch ends)
+FIELD_TRAFFIC_256 = 81.78e6
 
 
 def parse():
@@ -355,7 +359,9 @@ def run_ours(args):
         "calibration_sm_clock_mhz": clk.value / 1e6,
         "peak_nominal_at_sampled_clock": peak_nominal,
         "frac_of_nominal": per_gpu / peak_nominal if peak_nominal else None,
-        "traffic": None,
+        "traffic": FIELD_TRAFFIC_256 if count == 256 else None,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one 256^3 launch",
+        "algorithmic_bytes": d2h + 48 * w.n,
         "hbm_write_gbs": d2h / (total_s / args.steps) / 1e9,
     }
 

@@ -175,7 +175,8 @@ int64_t AFC_ServeSubmitField(void *engine, int32_t geometry, const float *h_amps
 int64_t AFC_ServeSubmitGspat(void *engine, int32_t geometry, const float *h_foci,
                              const float *h_amps, uint64_t n_foci, const AfcGridDesc *slice,
                              float *h_slice_out, float *h_amp_phase_out);
-/* Blocks until the request has finished; its latency and time spent queued [s]. */
+/* Blocks until the request has finished; its latency and time spent queued [s].  Call it
+ * exactly once per request (from any one thread): it releases the request's record. */
 int32_t AFC_ServeWait(void *engine, int64_t request, double *latency_s, double *queue_s);
 int32_t AFC_ServeStats(void *engine, AfcServeStats *stats);
 /* Finishes queued and running requests, then frees the engine. */
