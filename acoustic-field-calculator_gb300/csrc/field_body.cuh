@@ -132,14 +132,14 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
     float2 xc;
     directivity2_fast(tab, make_float2(ct, ct), xc);
     if (!near_edge(xc.x)) return make_float2(0.f, 0.f);
-    const float th = acos2_fast(make_float2(ct, ct)).x;
-    const int i_fast = fast_bin(th);
+    const float thc = theta2_centred(make_float2(ct, ct)).x;
+    const int i_fast = fast_bin(thc);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
     if (i_exact == i_fast) return make_float2(0.f, 0.f);
     const float r = r2 * rinv;
     const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
     const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
-    const float corr = w0 * (dir_in_bin(tab, th, i_exact) - dir_in_bin(tab, th, i_fast));
+    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - dir_in_bin(tab, thc, i_fast));
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 

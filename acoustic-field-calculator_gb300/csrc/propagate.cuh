@@ -37,13 +37,16 @@ constexpr float kTwoPiHi = 6.28318548202514648f;     // float(2*pi)
 constexpr float kTwoPiLo = -1.7484555314695172e-7f;  // 2*pi - float(2*pi)
 // (u + 1.5 * 2^23) - 1.5 * 2^23 rounds |u| < 2^22 to the nearest integer with two FADDs.
 constexpr float kRoundMagic = 12582912.0f;
-// 2^23: for 0 <= q < 2^23, q + 2^23 rounded upward is 2^23 + ceil(q), whose bit pattern minus
-// that of 2^23 (0x4B000000) is ceil(q) as an integer.
+// 2^23: for 0 <= q < 2^23, q + 2^23 rounded upward is 2^23 + ceil(q), whose low mantissa bits
+// are ceil(q) as an integer (the bit pattern of 2^23 is 0x4B000000).
 constexpr float kTwo23 = 8388608.0f;
-constexpr int kTwo23Bits = 0x4B000000;
+// 2^23 - 1/2: for theta_c = theta + ANGLE_DIV / 2, theta_c / ANGLE_DIV + (2^23 - 1/2) rounded
+// upward is 2^23 + ceil(theta / ANGLE_DIV) (to within the rounding of theta_c).
+constexpr float kTwo23Half = 8388607.5f;
 // 10-degree directivity bins: ANGLE_DIV = PI / 18 (t4010a1.rs:71) and its reciprocal.
 constexpr float kAngleDiv = 3.14159265358979323846f / 18.0f;
 constexpr float kInvAngleDiv = 18.0f / 3.14159265358979323846f;
+constexpr float kHalfAngleDiv = 0.5f * kAngleDiv;
 // A fast theta closer than this to a bin edge [rad] takes the exact path.  The fast theta is
 // within ~3e-6 rad of the reference's (1.7e-6 from the polynomial, ~1e-6 from rsqrt and FMA
 // rounding in cos(theta)), so 1e-5 leaves a factor of three.
@@ -73,24 +76,50 @@ constexpr float kAcos3 = -0.04563731327652931f;
 constexpr float kAcos4 = 0.020052572712302208f;
 constexpr float kAcos5 = -0.0045999325811862946f;
 
-// T4010A1 directivity coefficients (t4010a1.rs:18-69) as (a, b, c, d) per bin.  Entry 0
-// (theta == 0) evaluates to 1 like the reference's `0 => 1.0` arm, entries 1 and 2 are the
-// constant-1 bins, and entry 10 (with the zero-filled entries after it) stands for every bin
-// above 9, which evaluates to 0.
-#define AFC_DIR_TABLE_INIT                                                                      \
-    {                                                                                           \
-        {1.0f, 0.f, 0.f, 0.f}, {1.0f, 0.f, 0.f, 0.f}, {1.0f, 0.f, 0.f, 0.f},                    \
-            {1.0f, -0.2633589359691162f, -2.586746661956269f, 0.0009174516976956062f},          \
-            {0.891250938f, -0.8910683499820542f, -1.0097633564074366f, 0.0001704413361662757f}, \
-            {0.707945784f, -1.1924098538381465f, -0.7167962799004945f, 4.362034715924911f},     \
-            {0.501187234f, -1.0439934287916925f, 0.027352097655185065f, -2.238476800444034f},   \
-            {0.354813389f, -0.7015151838490918f, 0.39509604454751995f, 1.274774620435337f},     \
-            {0.251188643f, -0.4471050803642494f, 1.0625664749725618f, -1.1276955684895724f},    \
-            {0.199526231f, -0.179254124486545f, 0.008242027161100222f, -0.9016569137759131f},   \
-            {0.f, 0.f, 0.f, 0.f},                                                               \
+// T4010A1 directivity (t4010a1.rs:18-69) as (A, B, C, D) per bin: the reference's cubic
+// a + (b + (c + d x) x) x in x = theta - (i - 1) ANGLE_DIV re-expanded about the bin centre, in
+// xc = x - ANGLE_DIV / 2 (derived and checked to 6e-8 against the reference's own f32
+// evaluation in dir_table.py).  Entry 0 (theta == 0) evaluates to 1 like the reference's
+// `0 => 1.0` arm, entries 1 and 2 are the constant-1 bins, entries 10..30 stand for every bin
+// above 9 (0), and entry 31 (1) is where the rounded bin index wraps for theta within rounding
+// of 0.
+#define AFC_DIR_TABLE_INIT \
+    { \
+        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.ea25b8p-1f, -0x1.6dfba4p-1f, -0x1.4b12a6p+1f, 0x1.e10248p-11f},  \
+        {0x1.9c91eep-1f, -0x1.113aaap+0f, -0x1.027ceep+0f, 0x1.6570fep-13f},  \
+        {0x1.33e156p-1f, -0x1.37c58cp+0f, 0x1.b362dep-2f, 0x1.172b94p+2f},  \
+        {0x1.a29d0ep-2f, -0x1.1721dep+0f, -0x1.1e0b46p-1f, -0x1.1e8668p+1f},  \
+        {0x1.3096e8p-2f, -0x1.34f54ep-1f, 0x1.75296p-1f, 0x1.4657a2p+0f},  \
+        {0x1.c19078p-3f, -0x1.26505cp-2f, 0x1.88e054p-1f, -0x1.20b0a8p+0f},  \
+        {0x1.777e96p-3f, -0x1.965abp-3f, -0x1.d28ebp-3f, -0x1.cda5fap-1f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0.f, 0.f, 0.f, 0.f},  \
+        {0x1.0p+0f, 0.f, 0.f, 0.f} \
     }
-// The fast path indexes the table with the low five bits of 2^23 + ceil(theta / ANGLE_DIV)
-// (theta < 2.8 rad, so ceil(...) <= 16): entries 10..31 are zero like entry 10.
+// The fast path indexes the table with the low five bits of the rounded bin float (theta < 2.8
+// rad, so the bin is at most 16, or wraps to 31 just below 0).
 constexpr int kDirTableSize = 32;
 
 // ------------------------------------------------------------------ MUFU operations
@@ -144,9 +173,11 @@ static __device__ __noinline__ int exact_bin(float dx, float dy, float dz, float
            (c <= kBinCos9) + (c <= kBinCos10);
 }
 
-// Fast theta from cos(theta) for two points.  A c rounded above 1 gives sqrt(|1 - c|), a theta
-// of a few 1e-4 rad at most: bin 1, where the directivity is 1 as at theta = 0.
-__device__ __forceinline__ float2 acos2_fast(float2 ct) {
+// Fast theta + ANGLE_DIV / 2 (the bin-centred angle the directivity is evaluated from) from
+// cos(theta) for two points; the half bin rides on the final FMA for free.  A c rounded above
+// 1 gives sqrt(|1 - c|), a theta of a few 1e-4 rad at most: bin 1, where the directivity is 1
+// as at theta = 0.
+__device__ __forceinline__ float2 theta2_centred(float2 ct) {
     const float2 c = ct;
     const float2 om = fma2(c, f2(-1.0f), f2(1.0f));  // 1 - c
     const float2 s = make_float2(mufu_sqrt(fabsf(om.x)), mufu_sqrt(fabsf(om.y)));
@@ -155,51 +186,50 @@ __device__ __forceinline__ float2 acos2_fast(float2 ct) {
     q = fma2(q, c, f2(kAcos2));
     q = fma2(q, c, f2(kAcos1));
     q = fma2(q, c, f2(kAcos0));
-    return mul2(s, q);
+    return fma2(s, q, f2(kHalfAngleDiv));
 }
 
-// The bin the fast path takes for theta th, ceil(th / ANGLE_DIV), clipped to 10 (the packed
-// form is in directivity2_fast; bins 10 and above all evaluate to 0).
-__device__ __forceinline__ int fast_bin(float th) {
-    const int i = __float_as_int(__fmaf_ru(th, kInvAngleDiv, kTwo23)) & (kDirTableSize - 1);
-    return i < 10 ? i : 10;
+// The table entry the fast path takes for the centred angle thc (the packed form is in
+// directivity2_fast): ceil(theta / ANGLE_DIV), 0..16, or 31 just below theta = 0.
+__device__ __forceinline__ int fast_bin(float thc) {
+    return __float_as_int(__fmaf_ru(thc, kInvAngleDiv, kTwo23Half)) & (kDirTableSize - 1);
 }
 
-// The cubic of bin i (0..10) at theta th.
-__device__ __forceinline__ float dir_in_bin(const float4* __restrict__ tab, float th, int i) {
+// The cubic of table entry i at the centred angle thc.
+__device__ __forceinline__ float dir_in_bin(const float4* __restrict__ tab, float thc, int i) {
     const float4 c = tab[i];
-    const float x = fmaf(static_cast<float>(i - 1), -kAngleDiv, th);
-    return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
+    const float xc = fmaf(static_cast<float>(i), -kAngleDiv, thc);
+    return fmaf(fmaf(fmaf(c.w, xc, c.z), xc, c.y), xc, c.x);
 }
 
-// Directivity of one pair whose fast theta th fell next to a bin edge: the exact bin's cubic.
-__device__ __forceinline__ float directivity_exact(const float4* __restrict__ tab, float th,
+// Directivity of one pair whose fast theta fell next to a bin edge: the exact bin's cubic at
+// the fast centred angle thc.
+__device__ __forceinline__ float directivity_exact(const float4* __restrict__ tab, float thc,
                                                    float dx, float dy, float dz, float nx,
                                                    float ny, float nz) {
-    return dir_in_bin(tab, th, exact_bin(dx, dy, dz, nx, ny, nz));
+    return dir_in_bin(tab, thc, exact_bin(dx, dy, dz, nx, ny, nz));
 }
 
 // Bin lookup and cubic for one point given 2^23 + ceil(theta / ANGLE_DIV) (whose low five bits
-// are the bin) and x = theta - (bin - 1) ANGLE_DIV.
+// are the table entry) and xc, theta's offset from the centre of that bin.
 __device__ __forceinline__ float dir_cubic(const float4* __restrict__ tab, float fq_biased,
-                                           float x) {
+                                           float xc) {
     const float4 c = tab[__float_as_int(fq_biased) & (kDirTableSize - 1)];
-    return fmaf(fmaf(fmaf(c.w, x, c.z), x, c.y), x, c.x);
+    return fmaf(fmaf(fmaf(c.w, xc, c.z), xc, c.y), xc, c.x);
 }
 
 // Fast directivity of two points (packed) from their cos(theta).  `xc` receives each point's
-// offset from the centre of its bin: |xc| > kEdgeBound marks a theta within kEdgeMargin of a
-// bin edge, where the caller replaces the directivity by the exact bin's (testing every edge
-// costs fewer instructions than selecting the four where the directivity jumps, and the exact
-// bin gives the same D at the others).
+// offset from the centre of its bin, the cubic's variable: |xc| > kEdgeBound marks a theta
+// within kEdgeMargin of a bin edge, where the caller replaces the directivity by the exact
+// bin's (testing every edge costs fewer instructions than selecting the four where the
+// directivity jumps, and the exact bin gives the same D at the others).
 __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ tab, float2 ct,
                                                     float2& xc) {
-    const float2 th = acos2_fast(ct);
-    const float2 fq = __ffma2_ru(th, f2(kInvAngleDiv), f2(kTwo23));     // 2^23 + ceil(q)
-    const float2 fi = add2(fq, f2(-kTwo23));                             // ceil(q)
-    const float2 x = fma2(fi, f2(-kAngleDiv), add2(th, f2(kAngleDiv)));  // th - (fi-1) div
-    xc = add2(x, f2(-0.5f * kAngleDiv));
-    return make_float2(dir_cubic(tab, fq.x, x.x), dir_cubic(tab, fq.y, x.y));
+    const float2 thc = theta2_centred(ct);                                 // theta + div / 2
+    const float2 fq = __ffma2_ru(thc, f2(kInvAngleDiv), f2(kTwo23Half));  // 2^23 + ceil(q)
+    const float2 fi = add2(fq, f2(-kTwo23));                               // ceil(q)
+    xc = fma2(fi, f2(-kAngleDiv), thc);                                    // th - (fi - 1/2) div
+    return make_float2(dir_cubic(tab, fq.x, xc.x), dir_cubic(tab, fq.y, xc.y));
 }
 
 __device__ __forceinline__ bool near_edge(float xc) { return fabsf(xc) > kEdgeBound; }
@@ -212,9 +242,9 @@ __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, f
     float2 d = directivity2_fast(tab, ct, xc);
     const bool ex = near_edge(xc.x), ey = near_edge(xc.y);
     if (ex | ey) {
-        const float2 th = acos2_fast(ct);
-        if (ex) d.x = directivity_exact(tab, th.x, dx.x, dy.x, dz.x, nx, ny, nz);
-        if (ey) d.y = directivity_exact(tab, th.y, dx.y, dy.y, dz.y, nx, ny, nz);
+        const float2 thc = theta2_centred(ct);
+        if (ex) d.x = directivity_exact(tab, thc.x, dx.x, dy.x, dz.x, nx, ny, nz);
+        if (ey) d.y = directivity_exact(tab, thc.y, dx.y, dy.y, dz.y, nx, ny, nz);
     }
     return d;
 }
