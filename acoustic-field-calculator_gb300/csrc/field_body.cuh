@@ -52,7 +52,16 @@ struct SmemTile {
     float4 v0[kTile], v1[kTile], v2[kTile], v3[kTile], v4[kTile];
     float2 ns[kTile];
     float4 dir[kDirTableSize];
+    float box[kThreads / 32][6];  // per-warp bounds of the block's points (min xyz, max xyz)
+    float bbox[6];                // the block's bounds
 };
+
+// The phase phi + k r goes to sin/cos.approx unreduced when it is at most this large for every
+// source of a tile and every point of the block: the approximations take their argument in
+// turns after one FP32 multiply, whose rounding gives an absolute error of ~1.2e-7 |phase|
+// (<= 8e-5 rad here, the order of the reference's own f32 rounding of phi + k r); larger
+// phases are first reduced to [-pi, pi] (reduce_phase2).
+constexpr float kUnreducedPhaseMax = 640.0f;
 
 // Neumaier's compensated addition: sum + v with the lost low-order part added to comp.
 __device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
@@ -162,8 +171,9 @@ struct PairGeom {
 
 // The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
 // records whether any of the thread's points has its theta next to a bin edge; that rare case
-// recomputes the pairs' geometry to find which points, and corrects them one by one.
-template <int ST, int SUM, int PAIRS, bool UD>
+// recomputes the pairs' geometry to find which points, and corrects them one by one.  RED:
+// reduce the phase before sin/cos (see kUnreducedPhaseMax).
+template <int ST, int SUM, int PAIRS, bool UD, bool RED>
 __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, float3 n0,
                                                   float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
                                                   float2 (&PZ)[PAIRS], float2 (&NP)[PAIRS],
@@ -188,7 +198,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
             w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
             any_near |= near_edge(xc.x) | near_edge(xc.y);
         }
-        const float2 red = reduce_phase2(hi2(v1), r, hi2(v4));
+        const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
         const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
         if constexpr (SUM == SUM_PLAIN) {
@@ -256,6 +266,43 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
         const float4 b0 = src[0].b;
         n0 = make_float3(b0.x, b0.y, b0.z);
     }
+    // bounding box of the block's points (for the phase bound of each source tile)
+    float bmin[3] = {PX[0].x, PY[0].x, PZ[0].x}, bmax[3] = {PX[0].x, PY[0].x, PZ[0].x};
+#pragma unroll
+    for (int k = 1; k < kPPT; ++k) {
+        const float c[3] = {lane_of(PX[k >> 1], k & 1), lane_of(PY[k >> 1], k & 1),
+                            lane_of(PZ[k >> 1], k & 1)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            bmin[a] = fminf(bmin[a], c[a]);
+            bmax[a] = fmaxf(bmax[a], c[a]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            bmin[a] = fminf(bmin[a], __shfl_xor_sync(0xffffffffu, bmin[a], o));
+            bmax[a] = fmaxf(bmax[a], __shfl_xor_sync(0xffffffffu, bmax[a], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            sm.box[threadIdx.x >> 5][a] = bmin[a];
+            sm.box[threadIdx.x >> 5][3 + a] = bmax[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int a = threadIdx.x;
+        float v = sm.box[0][a];
+#pragma unroll
+        for (int w = 1; w < kThreads / 32; ++w) v = a < 3 ? fminf(v, sm.box[w][a]) : fmaxf(v, sm.box[w][a]);
+        sm.bbox[a] = v;
+    }
+    __syncthreads();  // sm.bbox is read while staging each tile below
+
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         NP[q] = fma2(f2(n0.z), PZ[q], fma2(f2(n0.y), PY[q], mul2(f2(n0.x), PX[q])));
@@ -268,9 +315,15 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
     for (int64_t t0 = 0; t0 < n; t0 += kTile) {
         const int cnt = static_cast<int>((n - t0) < kTile ? (n - t0) : kTile);
         __syncthreads();
-        bool same_dir = true;
+        bool same_dir = true, small_phase = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
             const PackedSource s = src[t0 + j];
+            // |phi' + k r| over the box: r is at most the distance to the farthest corner
+            const float fx = fmaxf(fabsf(sm.bbox[0] - s.a.x), fabsf(sm.bbox[3] - s.a.x));
+            const float fy = fmaxf(fabsf(sm.bbox[1] - s.a.y), fabsf(sm.bbox[4] - s.a.y));
+            const float fz = fmaxf(fabsf(sm.bbox[2] - s.a.z), fabsf(sm.bbox[5] - s.a.z));
+            const float rmax = sqrtf(fmaf(fz, fz, fmaf(fy, fy, fx * fx)));
+            small_phase = small_phase && fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y)) <= kUnreducedPhaseMax;
             sm.v0[j] = make_float4(-s.a.x, -s.a.x, -s.a.y, -s.a.y);
             sm.v1[j] = make_float4(-s.a.z, -s.a.z, s.a.w, s.a.w);
             sm.v2[j] = make_float4(s.b.x, s.b.x, s.b.y, s.b.y);
@@ -281,14 +334,31 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
             same_dir = same_dir && s.b.x == n0.x && s.b.y == n0.y && s.b.z == n0.z;
         }
         const bool tile_same_dir = __syncthreads_and(same_dir);
+        const bool tile_small = __syncthreads_and(small_phase);
         if (ST == SRC_T4010A1 && tile_same_dir) {
+            if (tile_small) {
 #pragma unroll 1
-            for (int j = 0; j < cnt; ++j)
-                accumulate_source<ST, SUM, PAIRS, true>(sm, j, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+                for (int j = 0; j < cnt; ++j)
+                    accumulate_source<ST, SUM, PAIRS, true, false>(sm, j, n0, PX, PY, PZ, NP, RE,
+                                                                   IM, CRE, CIM);
+            } else {
+#pragma unroll 1
+                for (int j = 0; j < cnt; ++j)
+                    accumulate_source<ST, SUM, PAIRS, true, true>(sm, j, n0, PX, PY, PZ, NP, RE, IM,
+                                                                  CRE, CIM);
+            }
         } else {
+            if (tile_small) {
 #pragma unroll 1
-            for (int j = 0; j < cnt; ++j)
-                accumulate_source<ST, SUM, PAIRS, false>(sm, j, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+                for (int j = 0; j < cnt; ++j)
+                    accumulate_source<ST, SUM, PAIRS, false, false>(sm, j, n0, PX, PY, PZ, NP, RE,
+                                                                    IM, CRE, CIM);
+            } else {
+#pragma unroll 1
+                for (int j = 0; j < cnt; ++j)
+                    accumulate_source<ST, SUM, PAIRS, false, true>(sm, j, n0, PX, PY, PZ, NP, RE,
+                                                                   IM, CRE, CIM);
+            }
         }
     }
 
