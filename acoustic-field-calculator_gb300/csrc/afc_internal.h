@@ -55,6 +55,18 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
                          const PointSet& ps, void* out, cudaStream_t s);
 
+// The rows tiling of a grid for `pairs` point pairs per thread (blocks of 1 << tx_log2
+// first-axis indices by (256 >> tx_log2) * 2 * pairs second-axis indices, one plane each), and
+// whether to use it: grids with more than one point along their second axis whose tiles keep at
+// least 90 % as many threads busy as the flat numbering.
+struct RowsTiling {
+    bool use;
+    int tx_log2;
+    int64_t rows;  // second-axis indices per tile
+    int64_t tiles0, tiles1, blocks;
+};
+RowsTiling rows_tiling(const GridDev& g, int64_t m, int pairs);
+
 // Packed sources of a request: geometry from `geom`, amplitude and phase from `amps` and
 // `phases` or, when `amp_phase` is not NULL, from its interleaved (amp, phase) pairs.
 cudaError_t launch_repack(const PackedSource* geom, const float* amps, const float* phases,

@@ -14,9 +14,12 @@
 //   * Each thread owns 2*PAIRS observation points spaced kThreads apart and processes them two
 //     at a time with the sm_100 packed FP32 instructions (FFMA2 / FMUL2 / FADD2), which halves
 //     the FP32 instructions issued; MUFU operations stay per point.  The PAIRS pairs of one
-//     source are independent, so their instructions interleave; the rare pairs whose theta
-//     lies next to a directivity bin edge are collected in a bit mask and corrected after the
-//     source, off the interleaved path.
+//     source are independent, so their instructions interleave; when any of a thread's
+//     points has its theta next to a directivity bin edge (a single predicate), those points
+//     are corrected after the source, off the interleaved path.
+//   * On grids with more than one point along the second axis a thread's points are
+//     consecutive along that axis (field_rows_kernel), so the offsets along the other two axes
+//     are computed once per source and thread.
 //   * When every source of a tile points the same way as source 0 (a planar array), cos(theta)
 //     comes from n.x - n.s with n.x precomputed per point and n.s per source: two FP32
 //     operations per pair instead of four.  Each block decides this per tile.
@@ -28,6 +31,7 @@
 
 #include "afc_internal.h"
 #include "field_body.cuh"
+#include "field_rows.cuh"
 #include "propagate.cuh"
 
 namespace afc {
@@ -49,6 +53,17 @@ __global__ void __launch_bounds__(kThreads, 2)
     block_points<ST, SUM, PAIRS>(sm, src, n, GRID, g, pts, m, first, field, out);
 }
 
+// Grids with more than one point along their second axis: tiles of TX = 1 << tx_log2 first-axis
+// indices by (kThreads / TX) * 2 * PAIRS second-axis indices, one plane each (field_rows.cuh).
+template <int ST, int SUM, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_rows_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g, int tx_log2,
+                      int64_t tiles0, int64_t tiles1, int field, void* __restrict__ out) {
+    __shared__ SmemTile sm;
+    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
+    block_rows<ST, SUM, PAIRS>(sm, src, n, g, tx_log2, tiles0, tiles1, blockIdx.x, field, out);
+}
+
 __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
                                     const float* __restrict__ k, const float* __restrict__ atten,
                                     int64_t n, PackedSource* __restrict__ out) {
@@ -63,6 +78,16 @@ template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
                          void* out, cudaStream_t s) {
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
+    if (ps.is_grid) {
+        const RowsTiling t = rows_tiling(ps.grid, ps.m, PAIRS);
+        if (t.use) {
+            if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+            field_rows_kernel<ST, SUM, PAIRS><<<static_cast<unsigned>(t.blocks), kThreads, 0, s>>>(
+                src, n, ps.grid, t.tx_log2, t.tiles0, t.tiles1, field, out);
+            count_launch();
+            return cudaGetLastError();
+        }
+    }
     const int64_t blocks = (ps.m + per_block - 1) / per_block;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     if (ps.is_grid) {
@@ -92,6 +117,24 @@ cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const Po
 }  // namespace
 
 std::atomic<uint64_t> g_launches{0};
+
+RowsTiling rows_tiling(const GridDev& g, int64_t m, int pairs) {
+    RowsTiling t{false, 5, 0, 0, 0, 0};
+    if (g.count[1] <= 1 || m <= 0) return t;
+    // first-axis tile: the smallest power of two >= count[0], between 32 and kThreads
+    while (t.tx_log2 < 8 && (1LL << t.tx_log2) < g.count[0]) ++t.tx_log2;
+    t.rows = (static_cast<int64_t>(kThreads) >> t.tx_log2) * 2 * pairs;
+    t.tiles0 = (g.count[0] + (1LL << t.tx_log2) - 1) >> t.tx_log2;
+    t.tiles1 = (g.count[1] + t.rows - 1) / t.rows;
+    t.blocks = t.tiles0 * t.tiles1 * g.count[2];
+    // the tiles leave the threads past the grid's edges idle: take them only while they keep
+    // at least 90 % as many threads busy as the flat numbering does
+    const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * pairs;
+    const int64_t flat_blocks = (m + per_block - 1) / per_block;
+    t.use = 10 * flat_blocks >= 9 * t.blocks;
+    return t;
+}
+
 
 int num_sms() {
     if (g_num_sms == 0) {

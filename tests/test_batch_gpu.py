@@ -83,7 +83,9 @@ def test_batch_matches_one_by_one_and_oracle(gpu):
                 a_o = _as_field(o, jb.field_type)
                 assert np.all(np.isfinite(a_b))
                 peak = max(float(np.max(np.abs(a_o))), 1e-30) if a_o.size else 1.0
-                assert np.max(np.abs(a_b - a_o), initial=0.0) <= 1e-6 * peak
+                # one by one, grids may take the rows tiling, whose r^2 rounds differently from
+                # the persistent kernel's general body: equal to float rounding, not bit for bit
+                assert np.max(np.abs(a_b - a_o), initial=0.0) <= 1e-5 * peak
                 _check(jb, a_b, _oracle(jb, _points(jb, p)))
         finally:
             afc.DLL.AFC_BatchFree(plan)

@@ -325,3 +325,75 @@ def test_large_grid_subsample_vs_f64(gpu):
     print(f"large grid subsample ({len(idx)} pts): max err/peak vs f64 {e64:.2e}, vs f32 oracle "
           f"{e32:.2e}, oracle f32 vs f64 {rel_err(ref32, ref64):.2e}, rel-L2 vs f64 {rl2:.2e}")
     assert e64 <= TOL and e32 <= TOL
+
+
+@pytest.mark.parametrize("layout", ["all_far", "mixed_tiles"])
+def test_far_phases_take_the_reduced_path(gpu, layout):
+    """Phases above the kernels' unreduced bound (640 rad) are reduced to [-pi, pi] first, tile
+    by tile: every source tile 1 m from the points ("all_far", phases ~ 740-790 rad), or the
+    first tile of 256 near and the following tiles far ("mixed_tiles").  The drive focuses on
+    the observed region (the reference focal law), so the sum is coherent and both float32
+    paths are well within the bar of the float64 field; checked against the f32 and the f64
+    oracle, on a grid and on scatter points."""
+    afc = gpu
+    rng = np.random.default_rng(31)
+    n = 700
+    pos = rng.uniform(-60, 60, (n, 3)).astype(np.float32)
+    pos[:, 2] = rng.uniform(-5, 5, n)
+    if layout == "all_far":
+        pos[:, 2] -= 1000.0
+    else:
+        pos[256:, 2] -= 1000.0
+    rec = W.t4010a1_records(pos, rng.uniform(0.5, 1.0, n).astype(np.float32),
+                            W.focal_phases(pos, (0.0, 0.0, 120.0)))
+    k = np.full(n, W.wavenumber(), np.float32)
+    a = np.zeros(n, np.float32)
+    s = make_system(afc, 1, rec, k, a)
+    pts = rng.uniform(-40, 40, (3000, 3)).astype(np.float32)
+    pts[:, 2] = rng.uniform(100, 140, 3000)
+    g = W.GridSpec(2, [(-40.0, 40.25), (-40.0, 40.25), (120.0, 120.0)], 0.5, (1, 2, 3))
+    lo, hi = g.lo_hi()
+    gp = O.grid_points(2, lo, hi, 0.5, (1, 2, 3))
+    calc = afc.GpuCalculator()
+    for area, p in ((scatter(afc, pts), pts), (afc.grid_from_spec(g), gp)):
+        out = calc.calculate(s, area, afc.ComplexPressureFieldBuffer())
+        assert out.shape[0] == len(p)
+        assert rel_err(out, O.field_f32(1, rec, k, a, p, O.FIELD_COMPLEX)) <= TOL
+        assert rel_err(out, O.field_f64(1, rec, k, a, p)) <= TOL
+
+
+@pytest.mark.parametrize("dim,axes,counts", [
+    (3, (1, 2, 3), (64, 40, 3)), (3, (1, 3, 2), (64, 40, 3)), (3, (2, 1, 3), (64, 40, 3)),
+    (3, (2, 3, 1), (64, 40, 3)), (3, (3, 1, 2), (64, 40, 3)), (3, (3, 2, 1), (64, 40, 3)),
+    (2, (1, 2, 3), (128, 50, 1)), (2, (3, 1, 2), (250, 17, 1)), (3, (1, 2, 3), (256, 256, 10)),
+])
+@pytest.mark.parametrize("tilted", [False, True])
+def test_rows_tiling(gpu, dim, axes, counts, tilted):
+    """Grids evaluated by the rows kernel (a thread's points consecutive along the second axis,
+    offsets along the other two shared): every axis order, counts that leave partial tiles, and
+    (256 x 256 x 10) enough points for four point pairs per thread; sources facing one way or
+    tilted (per-source directions)."""
+    afc = gpu
+    rng = np.random.default_rng(sum(counts) + dim + 3 * tilted)
+    n = 300
+    rec, k, a = random_sources(rng, 1, n)
+    if not tilted:
+        rec[:, 3:6] = (0.0, 0.0, 1.0)
+    res = 0.75
+    origin = {1: -30.0, 2: -20.0, 3: 70.0}
+    spec = []
+    for j, ax in enumerate(axes):
+        lo_ = origin[ax]
+        spec.append((lo_, lo_ + (counts[j] - 1) * res + 0.5 * res) if j < dim else (lo_, lo_))
+    g = W.GridSpec(dim, spec, res, axes)
+    s = make_system(afc, 1, rec, k, a)
+    area = afc.grid_from_spec(g)
+    assert tuple(int(c) for c in area.grid_desc().count) == tuple(counts[:dim]) + (1,) * (3 - dim)
+    lo, hi = g.lo_hi()
+    pts = O.grid_points(dim, lo, hi, res, axes)
+    out = afc.GpuCalculator().calculate(s, area, afc.ComplexPressureFieldBuffer())
+    assert out.shape[0] == len(pts)
+    sel = np.arange(len(pts)) if len(pts) <= 40000 else np.random.default_rng(1).choice(
+        len(pts), 40000, replace=False)
+    ref = O.field_f32(1, rec, k, a, pts[sel], O.FIELD_COMPLEX)
+    assert rel_err(out[sel], ref) <= TOL
