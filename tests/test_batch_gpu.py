@@ -84,8 +84,10 @@ def test_batch_matches_one_by_one_and_oracle(gpu):
                 assert np.all(np.isfinite(a_b))
                 peak = max(float(np.max(np.abs(a_o))), 1e-30) if a_o.size else 1.0
                 # one by one, grids may take the rows tiling, whose r^2 rounds differently from
-                # the persistent kernel's general body: equal to float rounding, not bit for bit
-                assert np.max(np.abs(a_b - a_o), initial=0.0) <= 1e-5 * peak
+                # the persistent kernel's general body (and a one-ulp change of r moves an
+                # unreduced phase k r by ~1e-7 k r): the two agree to the parity bar, not bit for
+                # bit, and each is checked against the oracle below
+                assert np.max(np.abs(a_b - a_o), initial=0.0) <= (2 if jb.field_type == 1 else 1) * TOL * peak
                 _check(jb, a_b, _oracle(jb, _points(jb, p)))
         finally:
             afc.DLL.AFC_BatchFree(plan)
