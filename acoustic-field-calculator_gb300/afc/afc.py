@@ -440,6 +440,21 @@ class Optimizer:
         _dll().AFO_FocalPoint(system.handle, p, system._source_type)
 
     @staticmethod
+    def bessel(system: UniformSystem, p, direction, theta_z: float):
+        if not isinstance(p, Vector3):
+            p = Vector3(p)
+        if not isinstance(direction, Vector3):
+            direction = Vector3(direction)
+        _dll().AFO_BesselBeam(system.handle, p, direction, c_float(theta_z), system._source_type)
+
+    @staticmethod
+    def ifft(system: UniformSystem, path, bottom_left, top_left, bottom_right, spacing, z):
+        _dll().AFC_ClearLastError()
+        _dll().AFO_IFFT(system.handle, path.encode("utf-8"), bottom_left, top_left, bottom_right,
+                        spacing, z, system._source_type)
+        _check()
+
+    @staticmethod
     def _multi(fn_name, system, foci, amps, *extra):
         _dll().AFC_ClearLastError()
         keep = _foci_args(foci, amps)

@@ -818,7 +818,40 @@ void AFO_Naive(void* handle, const void* foci, const float* amps, uint64_t size,
     run_solver(SOLVER_NAIVE, handle, foci, amps, size, source_type);
 }
 
-void AFO_BesselBeam(void*, AfcVector3, AfcVector3, float, int32_t) { unsupported("AFO_BesselBeam"); }
+// bessel.rs:30-51 (Hasegawa et al. 2017): each source's phase from its offset to `point`,
+// rotated by asin|v| about v = (dir.y, -dir.x, 0) (Rodrigues' formula with nalgebra's cross
+// and dot orders), on a cone of half-angle theta: f32 host arithmetic, O(n) set-up.
+void AFO_BesselBeam(void* handle, AfcVector3 point, AfcVector3 dir, float theta,
+                    int32_t source_type) {
+    if (!valid_source_type(source_type)) {
+        set_error("unknown source type %d", source_type);
+        return;
+    }
+    System* s = as_system(handle, source_type);
+    if (!s) return;
+    const float vx = dir.y, vy = -dir.x, vz = 0.0f;
+    const float theta_w = asinf(sqrtf(vx * vx + vy * vy + vz * vz));
+    const float cw = cosf(theta_w), sw = sinf(theta_w), omc = 1.0f - cosf(theta_w);
+    const float st = sinf(theta), ct = cosf(theta);
+    const int stride = source_stride(source_type);
+    const int iphase = source_type == SRC_T4010A1 ? 7 : 4;
+    for (size_t j = 0; j < s->count(); ++j) {
+        float* rec = s->src.data() + stride * j;
+        const float rx = rec[0] - point.x, ry = rec[1] - point.y, rz = rec[2] - point.z;
+        // xr = r x v
+        const float xx = ry * vz - rz * vy, xy = rz * vx - rx * vz, xz = rx * vy - ry * vx;
+        const float vd = (vx * rx + vy * ry) + vz * rz;
+        const float f = vd * omc;
+        const float qx = (rx * cw + xx * sw) + vx * f;
+        const float qy = (ry * cw + xy * sw) + vy * f;
+        const float qz = (rz * cw + xz * sw) + vz * f;
+        const float dist = st * sqrtf(qx * qx + qy * qy) - ct * qz;
+        const float wave_length = s->c / rec[stride - 1];
+        float phase = fmodf(dist, wave_length) / wave_length;
+        phase = -2.0f * kPiF * phase;
+        rec[iphase] = phase;
+    }
+}
 void AFO_IFFT(void*, const char*, AfcVector3, AfcVector3, AfcVector3, float, float, int32_t) {
     unsupported("AFO_IFFT");
 }

@@ -383,6 +383,39 @@ ORC_EXPORT void oracle_focal_point(int st, float *src, int64_t n, float sound_sp
     }
 }
 
+/* bessel.rs:30-51: v = (dir.y, -dir.x, 0), theta_w = asin |v|; each source's offset
+ * r = pos - point is rotated, r' = r cos(theta_w) + (r x v) sin(theta_w) + v (v.r)(1 - cos(theta_w)),
+ * dist = sin(theta) |r'_xy| - cos(theta) r'_z, phase = -2 pi fmod(dist, lambda) / lambda.  f32 with
+ * nalgebra's component orders: cross (a.y b.z - a.z b.y, a.z b.x - a.x b.z, a.x b.y - a.y b.x),
+ * dot and norm^2 ((x x' + y y') + z z'). */
+ORC_EXPORT void oracle_bessel_beam(int st, float *src, int64_t n, float sound_speed, float px,
+                                   float py, float pz, float dx, float dy, float dz, float theta) {
+    (void)dz;
+    const int stride = src_stride(st);
+    const int iphase = st == ORC_SRC_T4010A1 ? 7 : 4;
+    const int ifreq = st == ORC_SRC_T4010A1 ? 8 : 5;
+    float v[3] = {dy, -dx, 0.0f};
+    float theta_w = asinf(sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]));
+    for (int64_t j = 0; j < n; ++j) {
+        float *s = src + stride * j;
+        float r[3] = {s[0] - px, s[1] - py, s[2] - pz};
+        float xr[3] = {r[1] * v[2] - r[2] * v[1], r[2] * v[0] - r[0] * v[2],
+                       r[0] * v[1] - r[1] * v[0]};
+        float vdr = (v[0] * r[0] + v[1] * r[1]) + v[2] * r[2];
+        float scale = vdr * (1.0f - cosf(theta_w));
+        float q[3];
+        for (int c = 0; c < 3; ++c) {
+            float a = r[c] * cosf(theta_w);
+            float b = xr[c] * sinf(theta_w);
+            q[c] = (a + b) + v[c] * scale;
+        }
+        float dist = sinf(theta) * sqrtf(q[0] * q[0] + q[1] * q[1]) - cosf(theta) * q[2];
+        float wave_length = sound_speed / s[ifreq];
+        float phase = fmodf(dist, wave_length) / wave_length;
+        s[iphase] = -2.0f * ORC_PI_F * phase;
+    }
+}
+
 /* ---------------------------------------------------------------- G and the solvers */
 
 /* macros.rs:32-53: G[i, j] = propagate(source j, focus i) with the sources' current amp and

@@ -63,6 +63,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_grid_points.argtypes = [c_int, fp, fp, c_float, POINTER(c_int), fp]
         L.oracle_grid_points.restype = c_int64
         L.oracle_focal_point.argtypes = [c_int, fp, c_int64, c_float, c_float, c_float, c_float]
+        L.oracle_bessel_beam.argtypes = [c_int, fp, c_int64, c_float] + [c_float] * 7
         L.oracle_build_g_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, fp]
         L.oracle_build_g_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, dp, c_int]
         L.oracle_gspat_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int, dp]
@@ -198,6 +199,15 @@ def focal_point(st, sources, sound_speed_, focus) -> np.ndarray:
     s = np.array(sources, dtype=np.float32, copy=True).reshape(-1)
     n = s.size // (9 if st == SRC_T4010A1 else 6)
     lib().oracle_focal_point(st, _f(s), n, sound_speed_, *map(float, focus))
+    return s
+
+
+def bessel_beam(st, sources, sound_speed_, point, direction, theta) -> np.ndarray:
+    """Sources with the Bessel-beam phases of bessel.rs:30-51 (f32)."""
+    s = np.array(sources, dtype=np.float32, copy=True).reshape(-1)
+    n = s.size // (9 if st == SRC_T4010A1 else 6)
+    lib().oracle_bessel_beam(st, _f(s), n, sound_speed_, *map(float, point),
+                             *map(float, direction), float(theta))
     return s
 
 

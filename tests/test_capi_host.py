@@ -97,6 +97,27 @@ def test_focal_point_matches_oracle(afc_mod):
     np.testing.assert_array_equal(s.records().reshape(-1), expect)
 
 
+@pytest.mark.parametrize("st", [0, 1])
+@pytest.mark.parametrize("direction,theta", [((0.0, 0.0, 1.0), 0.3), ((0.3, -0.2, 0.93), 0.15),
+                                             ((-0.5, 0.1, 0.86), 0.05)])
+def test_bessel_beam_matches_oracle(afc_mod, st, direction, theta):
+    """AFO_BesselBeam (host set-up, bessel.rs:30-51) equals the oracle bit for bit, for axial
+    and tilted beams, on both source types; other record fields are untouched."""
+    pos = W.tiled_array(2, 1)
+    rng = np.random.default_rng(5)
+    rec = (W.t4010a1_records if st == 1 else W.sphere_records)(
+        pos, rng.uniform(0.5, 1.0, len(pos)).astype(np.float32), 0.0)
+    s = _system(afc_mod, 293.0)
+    s.add_records(st, rec)
+    point = (90.0, 70.0, 0.0)
+    afc_mod.Optimizer.bessel(s, point, direction, theta)
+    expect = O.bessel_beam(st, rec, O.sound_speed(293.0), point, direction, theta)
+    np.testing.assert_array_equal(s.records().reshape(-1), expect)
+    iph = 7 if st == 1 else 4
+    assert np.all(np.abs(s.records()[:, iph]) <= 2 * np.pi)
+    assert np.ptp(s.records()[:, iph]) > 1.0  # the phases vary across the array
+
+
 @pytest.mark.parametrize("spec", [
     (1, [(0.0, 10.0), (3.0, 3.0), (4.0, 4.0)], 0.7, (2, 1, 3)),
     (2, [(36.36, 136.36), (16.04, 116.04), (150.0, 150.0)], 1.0, (1, 2, 3)),
