@@ -10,7 +10,10 @@
 
 namespace afc {
 
-enum SolverKind : int { SOLVER_GSPAT = 0, SOLVER_GS = 1, SOLVER_NAIVE = 2 };
+enum SolverKind : int { SOLVER_GSPAT = 0, SOLVER_GS = 1, SOLVER_NAIVE = 2, SOLVER_GREEDY = 3 };
+
+// Largest candidate-phase count of the greedy solver (one thread per candidate).
+constexpr int kGreedyMaxDiv = 1024;
 
 // REPEAT of gs_pat.rs:17 and gs.rs:17.
 constexpr int kSolverRepeat = 100;
@@ -34,10 +37,19 @@ cudaError_t launch_build_g(int st, const float* d_raw, const float* d_k, const f
                            int64_t n, const float* d_foci, int64_t m, float2* d_g,
                            void* ws_packed, cudaStream_t s);
 
+// Greedy phase choice (combination/greedy.rs:39-83) on the device: G is built as for the other
+// solvers, then one block takes the sources in order.  cand / cand_arg: the div candidate
+// phasors and their arguments (computed on the host).  Writes (amp, phase) per source to d_out.
+cudaError_t launch_greedy(int st, const float* d_raw, const float* d_k, const float* d_atten,
+                          int64_t n, const float* d_foci, const float* d_amps, int64_t m,
+                          const float2* d_cand, const float* d_cand_arg, int div, float* d_out,
+                          void* ws, cudaStream_t s);
+
 // Host-level: uploads, solves, and writes amp / phase into the host source array `src`
-// (ABI layout) in place.  Returns 0 on success, else fills *err.
+// (ABI layout) in place.  phase_div: candidate phases of SOLVER_GREEDY (1..kGreedyMaxDiv).
+// Returns 0 on success, else fills *err.
 int solve_multi_focus(int kind, int st, float* src, const float* k, const float* atten,
                       int64_t n, const float* foci, const float* amps, int64_t m,
-                      std::string* err);
+                      std::string* err, int phase_div = 0);
 
 }  // namespace afc

@@ -431,7 +431,7 @@ bool unpack_foci(const void* foci, const float* amps, uint64_t size, std::vector
 }
 
 void run_solver(int kind, void* handle, const void* foci, const float* amps, uint64_t size,
-                int32_t st) {
+                int32_t st, int phase_div = 0) {
     if (!valid_source_type(st)) {
         set_error("unknown source type %d", st);
         return;
@@ -443,7 +443,7 @@ void run_solver(int kind, void* handle, const void* foci, const float* amps, uin
     std::string err;
     const int rc = solve_multi_focus(kind, st, s->src.data(), s->k.data(), s->atten.data(),
                                      static_cast<int64_t>(s->count()), f.data(), a.data(),
-                                     static_cast<int64_t>(size), &err);
+                                     static_cast<int64_t>(size), &err, phase_div);
     if (rc != 0) set_error("%s", err.c_str());
 }
 
@@ -865,8 +865,13 @@ void AFO_GradientDescent(void*, const void*, const float*, uint64_t, int32_t) {
     unsupported("AFO_GradientDescent");
 }
 void AFO_LM(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_LM"); }
-void AFO_Greedy(void*, const void*, const float*, uint64_t, uint64_t, int32_t) {
-    unsupported("AFO_Greedy");
+void AFO_Greedy(void* handle, const void* foci, const float* amps, uint64_t size,
+                uint64_t phase_div, int32_t source_type) {
+    if (phase_div < 1 || phase_div > static_cast<uint64_t>(kGreedyMaxDiv)) {
+        set_error("AFO_Greedy: phase_div must be 1..%d", kGreedyMaxDiv);
+        return;
+    }
+    run_solver(SOLVER_GREEDY, handle, foci, amps, size, source_type, static_cast<int>(phase_div));
 }
 
 // ------------------------------------------------------------------ device-level API

@@ -33,6 +33,7 @@ namespace {
 __constant__ float4 c_dir_table_s[dev::kDirTableSize] = AFC_DIR_TABLE_INIT;
 
 constexpr int kIterThreads = 1024;
+constexpr float kPiF = 3.14159265358979323846f;  // f32 PI of the reference (core/mod.rs)
 
 size_t align256(size_t b) { return (b + 255) & ~static_cast<size_t>(255); }
 
@@ -243,6 +244,58 @@ __global__ void __launch_bounds__(kIterThreads)
     }
 }
 
+// Greedy (greedy.rs:39-83) in one block.  Source i (in order) tries every candidate phasor
+// c_k: thread k sums |amp_j - |G_ji c_k + cache_j|| over the foci j in order (f32, no
+// contraction, as the reference); the first minimum wins; cache_j += G_ji c_best.
+__global__ void __launch_bounds__(kIterThreads)
+    greedy_kernel(const float2* __restrict__ g, const PackedSource* __restrict__ src, int64_t n,
+                  int64_t m, const float* __restrict__ amps, const float2* __restrict__ cand,
+                  const float* __restrict__ cand_arg, int div, float2* cache,
+                  float* __restrict__ out) {
+    __shared__ float s_v[kGreedyMaxDiv];
+    __shared__ int s_best;
+    for (int64_t j = threadIdx.x; j < m; j += blockDim.x) cache[j] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int64_t i = 0; i < n; ++i) {
+        if (threadIdx.x < div) {
+            const float2 c = cand[threadIdx.x];
+            float v = 0.f;
+            for (int64_t j = 0; j < m; ++j) {
+                const float2 a = g[j * n + i];
+                const float2 t = make_float2(__fsub_rn(__fmul_rn(a.x, c.x), __fmul_rn(a.y, c.y)),
+                                             __fadd_rn(__fmul_rn(a.x, c.y), __fmul_rn(a.y, c.x)));
+                const float2 q = cache[j];
+                const float re = __fadd_rn(t.x, q.x), im = __fadd_rn(t.y, q.y);
+                v = __fadd_rn(v, fabsf(__fsub_rn(amps[j], hypotf(re, im))));
+            }
+            s_v[threadIdx.x] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int best = 0;
+            float min_v = __int_as_float(0x7f800000);  // +inf
+            for (int k = 0; k < div; ++k) {
+                if (s_v[k] < min_v) {
+                    min_v = s_v[k];
+                    best = k;
+                }
+            }
+            s_best = best;
+            out[2 * i] = src[i].c.z;
+            out[2 * i + 1] = cand_arg[best];
+        }
+        __syncthreads();
+        const float2 c = cand[s_best];
+        for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+            const float2 a = g[j * n + i];
+            const float2 t = make_float2(__fsub_rn(__fmul_rn(a.x, c.x), __fmul_rn(a.y, c.y)),
+                                         __fadd_rn(__fmul_rn(a.x, c.y), __fmul_rn(a.y, c.x)));
+            cache[j] = make_float2(__fadd_rn(cache[j].x, t.x), __fadd_rn(cache[j].y, t.y));
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void real_to_complex_kernel(const float* __restrict__ v, int64_t m,
                                        float2* __restrict__ out) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -279,6 +332,26 @@ cudaError_t launch_build_g(int st, const float* d_raw, const float* d_k, const f
         build_g_kernel<SRC_T4010A1><<<grid, 128, 0, s>>>(packed, n, d_foci, m, d_g);
     else
         build_g_kernel<SRC_SPHERE><<<grid, 128, 0, s>>>(packed, n, d_foci, m, d_g);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_greedy(int st, const float* d_raw, const float* d_k, const float* d_atten,
+                          int64_t n, const float* d_foci, const float* d_amps, int64_t m,
+                          const float2* d_cand, const float* d_cand_arg, int div, float* d_out,
+                          void* ws, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (m > kSolverMaxFoci || div < 1 || div > kGreedyMaxDiv) return cudaErrorInvalidValue;
+    SolverWs w = carve(ws, n, m);
+    cudaError_t e = launch_build_g(st, d_raw, d_k, d_atten, n, d_foci, m, w.g, w.packed, s);
+    if (e != cudaSuccess) return e;
+    if (m == 0) {
+        // no foci: launch_build_g did nothing; the packed sources still carry the amplitudes
+        if ((e = launch_pack_sources(st, d_raw, d_k, d_atten, n, w.packed, s)) != cudaSuccess)
+            return e;
+    }
+    greedy_kernel<<<1, kIterThreads, 0, s>>>(w.g, w.packed, n, m, d_amps, d_cand, d_cand_arg, div,
+                                             w.p, d_out);
     count_launch();
     return cudaGetLastError();
 }
@@ -351,9 +424,14 @@ cudaError_t grow_dev(void** p, size_t* cap, size_t bytes) {
 
 int solve_multi_focus(int kind, int st, float* src, const float* k, const float* atten,
                       int64_t n, const float* foci, const float* amps, int64_t m,
-                      std::string* err) {
+                      std::string* err, int phase_div) {
     if (m > kSolverMaxFoci) {
         *err = "too many foci (" + std::to_string(m) + " > " + std::to_string(kSolverMaxFoci) + ")";
+        return -1;
+    }
+    const bool greedy = kind == SOLVER_GREEDY;
+    if (greedy && (phase_div < 1 || phase_div > kGreedyMaxDiv)) {
+        *err = "phase_div must be 1.." + std::to_string(kGreedyMaxDiv);
         return -1;
     }
     if (n == 0) return 0;
@@ -379,8 +457,11 @@ int solve_multi_focus(int kind, int st, float* src, const float* k, const float*
     }
     if ((e = cudaSetDevice(c.device)) != cudaSuccess) return fail("cudaSetDevice");
     const int stride = source_stride(st);
-    // input block: raw | k | atten | foci | amps ; output: 2n floats
-    const size_t in_floats = static_cast<size_t>(n) * (stride + 2) + 4 * static_cast<size_t>(m);
+    // input block: raw | k | atten | foci | amps [| candidate phasors | their arguments, from a
+    // 16-byte boundary] ; output: 2n floats
+    const size_t base_floats = static_cast<size_t>(n) * (stride + 2) + 4 * static_cast<size_t>(m);
+    const size_t cand_off = (base_floats + 3) & ~static_cast<size_t>(3);
+    const size_t in_floats = greedy ? cand_off + 3 * static_cast<size_t>(phase_div) : base_floats;
     const size_t io_floats = in_floats > static_cast<size_t>(2 * n) ? in_floats : 2 * n;
     if (io_floats * sizeof(float) > c.h_io_cap) {
         if (c.h_io) cudaFreeHost(c.h_io);
@@ -397,6 +478,17 @@ int solve_multi_focus(int kind, int st, float* src, const float* k, const float*
     memcpy(h + n * (stride + 1), atten, sizeof(float) * n);
     memcpy(h + n * (stride + 2), foci, sizeof(float) * 3 * m);
     memcpy(h + n * (stride + 2) + 3 * m, amps, sizeof(float) * m);
+    if (greedy) {
+        // greedy.rs:21-27: exp(i 2 pi k / phase_div) in f32 (num-complex exp = from_polar(e^0, a))
+        // and, for set_phase, their arguments (greedy.rs:79)
+        float* hc = h + cand_off;
+        for (int q = 0; q < phase_div; ++q) {
+            const float a = 2.0f * kPiF * static_cast<float>(q) / static_cast<float>(phase_div);
+            hc[2 * q] = 1.0f * cosf(a);
+            hc[2 * q + 1] = 1.0f * sinf(a);
+            hc[2 * phase_div + q] = atan2f(hc[2 * q + 1], hc[2 * q]);
+        }
+    }
     const size_t in_bytes = align256(in_floats * sizeof(float)) + align256(2 * n * sizeof(float));
     if ((e = grow_dev(&c.d_in, &c.d_in_cap, in_bytes)) != cudaSuccess) return fail("cudaMalloc");
     if ((e = grow_dev(&c.d_ws, &c.d_ws_cap, solver_workspace_bytes(n, m))) != cudaSuccess)
@@ -407,8 +499,15 @@ int solve_multi_focus(int kind, int st, float* src, const float* k, const float*
     if ((e = cudaMemcpyAsync(d, h, in_floats * sizeof(float), cudaMemcpyHostToDevice, c.stream)) !=
         cudaSuccess)
         return fail("cudaMemcpyAsync");
-    e = launch_solver(kind, st, d, d + n * stride, d + n * (stride + 1), n, d + n * (stride + 2),
-                      d + n * (stride + 2) + 3 * m, m, kSolverRepeat, d_out, c.d_ws, c.stream);
+    if (greedy)
+        e = launch_greedy(st, d, d + n * stride, d + n * (stride + 1), n, d + n * (stride + 2),
+                          d + n * (stride + 2) + 3 * m, m,
+                          reinterpret_cast<const float2*>(d + cand_off),
+                          d + cand_off + 2 * phase_div, phase_div, d_out, c.d_ws, c.stream);
+    else
+        e = launch_solver(kind, st, d, d + n * stride, d + n * (stride + 1), n,
+                          d + n * (stride + 2), d + n * (stride + 2) + 3 * m, m, kSolverRepeat,
+                          d_out, c.d_ws, c.stream);
     if (e != cudaSuccess) return fail("solver launch");
     if ((e = cudaMemcpyAsync(h, d_out, 2 * n * sizeof(float), cudaMemcpyDeviceToHost, c.stream)) !=
         cudaSuccess)

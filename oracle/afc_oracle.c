@@ -416,6 +416,61 @@ ORC_EXPORT void oracle_bessel_beam(int st, float *src, int64_t n, float sound_sp
     }
 }
 
+/* ---------------------------------------------------------------- greedy
+ * combination/greedy.rs:21-83 in f32: every phase set to 0; candidates exp(i 2 pi k / div)
+ * (from_polar(e^0, a)); source by source, each candidate's sum over foci of
+ * |amp_j - |propagate(i, focus_j) * c_k + cache_j|| (complex norm = hypot), the first minimum
+ * kept, cache += its terms, phase_i = arg of the chosen candidate. */
+ORC_EXPORT void oracle_greedy_f32(int st, float *src, const float *k, const float *atten, int64_t n,
+                                  const float *foci, const float *amps, int64_t m, int div) {
+    const int stride = src_stride(st);
+    const int iphase = st == ORC_SRC_T4010A1 ? 7 : 4;
+    float *cre = (float *)calloc((size_t)(m > 0 ? m : 1), sizeof(float));
+    float *cim = (float *)calloc((size_t)(m > 0 ? m : 1), sizeof(float));
+    float *pre = (float *)malloc(sizeof(float) * (size_t)div);
+    float *pim = (float *)malloc(sizeof(float) * (size_t)div);
+    float *tre = (float *)malloc(sizeof(float) * (size_t)(m > 0 ? m : 1) * (size_t)div);
+    float *tim = (float *)malloc(sizeof(float) * (size_t)(m > 0 ? m : 1) * (size_t)div);
+    for (int q = 0; q < div; ++q) {
+        float a = 2.0f * ORC_PI_F * (float)q / (float)div;
+        pre[q] = 1.0f * cosf(a);
+        pim[q] = 1.0f * sinf(a);
+    }
+    for (int64_t j = 0; j < n; ++j) src[stride * j + iphase] = 0.0f;
+    for (int64_t i = 0; i < n; ++i) {
+        int best = 0;
+        float min_v = INFINITY;
+        for (int q = 0; q < div; ++q) {
+            float v = 0.0f;
+            for (int64_t j = 0; j < m; ++j) {
+                float gr, gi;
+                prop_f32(st, src + stride * i, k[i], atten[i], foci[3 * j], foci[3 * j + 1],
+                         foci[3 * j + 2], &gr, &gi);
+                float tr = gr * pre[q] - gi * pim[q];
+                float ti = gr * pim[q] + gi * pre[q];
+                tre[q * m + j] = tr;
+                tim[q * m + j] = ti;
+                v += fabsf(amps[j] - hypotf(tr + cre[j], ti + cim[j]));
+            }
+            if (v < min_v) {
+                min_v = v;
+                best = q;
+            }
+        }
+        for (int64_t j = 0; j < m; ++j) {
+            cre[j] += tre[best * m + j];
+            cim[j] += tim[best * m + j];
+        }
+        src[stride * i + iphase] = atan2f(pim[best], pre[best]);
+    }
+    free(cre);
+    free(cim);
+    free(pre);
+    free(pim);
+    free(tre);
+    free(tim);
+}
+
 /* ---------------------------------------------------------------- G and the solvers */
 
 /* macros.rs:32-53: G[i, j] = propagate(source j, focus i) with the sources' current amp and

@@ -64,6 +64,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_grid_points.restype = c_int64
         L.oracle_focal_point.argtypes = [c_int, fp, c_int64, c_float, c_float, c_float, c_float]
         L.oracle_bessel_beam.argtypes = [c_int, fp, c_int64, c_float] + [c_float] * 7
+        L.oracle_greedy_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int]
         L.oracle_build_g_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, fp]
         L.oracle_build_g_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, dp, c_int]
         L.oracle_gspat_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int, dp]
@@ -208,6 +209,18 @@ def bessel_beam(st, sources, sound_speed_, point, direction, theta) -> np.ndarra
     n = s.size // (9 if st == SRC_T4010A1 else 6)
     lib().oracle_bessel_beam(st, _f(s), n, sound_speed_, *map(float, point),
                              *map(float, direction), float(theta))
+    return s
+
+
+def greedy_f32(st, sources, k, atten, foci, amps, phase_div=16) -> np.ndarray:
+    """Sources with the greedy solver's phases (greedy.rs:39-83, f32)."""
+    s = np.array(sources, dtype=np.float32, copy=True).reshape(-1)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    atten = np.ascontiguousarray(atten, dtype=np.float32)
+    foci = np.ascontiguousarray(foci, dtype=np.float32).reshape(-1, 3)
+    amps = np.ascontiguousarray(amps, dtype=np.float32)
+    lib().oracle_greedy_f32(st, _f(s), _f(k), _f(atten), len(k), _f(foci), _f(amps), len(amps),
+                            int(phase_div))
     return s
 
 

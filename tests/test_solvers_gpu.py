@@ -98,3 +98,48 @@ def test_empty_focus_list(gpu):
     s = _system(afc, w)
     afc.Optimizer.gs_pat(s, np.zeros((0, 3), np.float32), np.zeros(0, np.float32))
     assert np.all(s.records()[:, 6] == 0)
+
+
+@pytest.mark.parametrize("m,div", [(2, 16), (8, 16), (8, 4), (31, 32)])
+def test_greedy_matches_oracle(gpu, m, div):
+    """AFO_Greedy (combination/greedy.rs:39-83) against the oracle's f32 restatement on 996
+    sources.  Each source's choice depends on all earlier ones, and the device's transfer matrix
+    comes from the fast (MUFU) pair math, so a near tie between two candidates can resolve the
+    other way and change every later choice (with few foci, once their targets are met many
+    candidates tie).  The bar is on the result: the achieved objective sum_j |amp_j -
+    |p(focus_j)|| (float64 field) no worse than the oracle's by more than 10 %, choices identical
+    far above chance (1 / div), amplitudes untouched and every phase a candidate's."""
+    afc = gpu
+    rng = np.random.default_rng(70 + m + div)
+    w, foci, amps = W.gspat_request(rng, m)
+    s = _system(afc, w)
+    afc.Optimizer.greedy(s, foci, amps, div)
+    got = s.records().copy()
+    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
+        ref = O.greedy_f32(1, w.sources, w.k, w.atten, foci, amps, div).reshape(-1, 9)
+    np.testing.assert_array_equal(got[:, 6], w.sources[:, 6])
+    cands = np.unique(ref[:, 7])
+    assert np.all(np.isin(got[:, 7], cands)) or div > len(cands)
+    same = float(np.mean(got[:, 7] == ref[:, 7]))
+    p_gpu = np.abs(O.field_f64(1, got, w.k, w.atten, foci))
+    p_ref = np.abs(O.field_f64(1, ref, w.k, w.atten, foci))
+    obj_gpu = float(np.sum(np.abs(amps - p_gpu)))
+    obj_ref = float(np.sum(np.abs(amps - p_ref)))
+    print(f"greedy m={m} div={div}: identical choices {same:.3f}, objective {obj_gpu:.4e} vs "
+          f"oracle {obj_ref:.4e}")
+    assert same >= 0.3
+    assert obj_gpu <= 1.1 * obj_ref + 1e-2 * float(np.sum(amps))
+
+
+def test_greedy_edge_cases(gpu):
+    afc = gpu
+    rng = np.random.default_rng(5)
+    w, foci, amps = W.gspat_request(rng, 4)
+    s = _system(afc, w)
+    afc.Optimizer.greedy(s, np.zeros((0, 3), np.float32), np.zeros(0, np.float32), 8)
+    rec = s.records()
+    assert np.all(rec[:, 7] == 0.0) and np.array_equal(rec[:, 6], w.sources[:, 6])
+    before = rec.copy()
+    with pytest.raises(RuntimeError, match="phase_div"):
+        afc.Optimizer.greedy(s, foci, amps, 0)
+    np.testing.assert_array_equal(s.records(), before)
