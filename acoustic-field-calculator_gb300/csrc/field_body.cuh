@@ -232,18 +232,20 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
     }
 }
 
-// One block of 2*PAIRS*kThreads observation points starting at point `first`: stage the n
-// sources tile by tile into `sm` (its dir table must already be filled), accumulate, apply
-// the field transform and store.  `grid` selects generated grid points or explicit ones.
+// One block of 2*PAIRS*kThreads observation points starting at point `first`: stage sources
+// s_lo .. s_hi - 1 tile by tile into `sm` (its dir table must already be filled) and accumulate
+// their fields into RE, IM (CRE, CIM: compensation terms).  `grid` selects generated grid
+// points or explicit ones; source 0's direction is the shared direction of the fast cos(theta).
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* __restrict__ src,
-                                             int64_t n, bool grid, const GridDev& g,
-                                             const float* __restrict__ pts, int64_t m,
-                                             int64_t first, int field, void* __restrict__ out) {
+__device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSource* __restrict__ src,
+                                                 int64_t n, int64_t s_lo, int64_t s_hi, bool grid,
+                                                 const GridDev& g, const float* __restrict__ pts,
+                                                 int64_t m, int64_t first, float2 (&RE)[PAIRS],
+                                                 float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                                 float2 (&CIM)[PAIRS]) {
     constexpr int kPPT = 2 * PAIRS;
     const int64_t base = first + threadIdx.x;
     float2 PX[PAIRS], PY[PAIRS], PZ[PAIRS], NP[PAIRS];
-    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         int64_t p = base + static_cast<int64_t>(k) * kThreads;
@@ -312,8 +314,8 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
         CIM[q] = f2(0.f);
     }
 
-    for (int64_t t0 = 0; t0 < n; t0 += kTile) {
-        const int cnt = static_cast<int>((n - t0) < kTile ? (n - t0) : kTile);
+    for (int64_t t0 = s_lo; t0 < s_hi; t0 += kTile) {
+        const int cnt = static_cast<int>((s_hi - t0) < kTile ? (s_hi - t0) : kTile);
         __syncthreads();
         bool same_dir = true, small_phase = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
@@ -361,7 +363,16 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
             }
         }
     }
+}
 
+// Apply the field transform to a block's sums (block_accumulate) and store them.
+template <int SUM, int PAIRS>
+__device__ __forceinline__ void block_store(float2 (&RE)[PAIRS], float2 (&IM)[PAIRS],
+                                            float2 (&CRE)[PAIRS], float2 (&CIM)[PAIRS],
+                                            int64_t first, int64_t m, int field,
+                                            void* __restrict__ out) {
+    constexpr int kPPT = 2 * PAIRS;
+    const int64_t base = first + threadIdx.x;
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         const int64_t p = base + static_cast<int64_t>(k) * kThreads;
@@ -380,6 +391,18 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
             reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
         }
     }
+}
+
+// One block of 2*PAIRS*kThreads observation points starting at point `first`, all n sources:
+// accumulate, apply the field transform and store.
+template <int ST, int SUM, int PAIRS>
+__device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* __restrict__ src,
+                                             int64_t n, bool grid, const GridDev& g,
+                                             const float* __restrict__ pts, int64_t m,
+                                             int64_t first, int field, void* __restrict__ out) {
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    block_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE, CIM);
+    block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
 }
 
 }  // namespace fb

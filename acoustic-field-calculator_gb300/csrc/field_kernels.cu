@@ -25,6 +25,11 @@
 //     operations per pair instead of four.  Each block decides this per tile.
 //   * Each of the 2*PAIRS stores is one contiguous, coalesced warp store (4 B or 8 B a point).
 //   * Grid points are generated from the grid description, never read from memory.
+//   * Launches too small to give every SM two blocks split each point tile's sources over the
+//     blocks of a thread-block cluster (field_split_kernel): rank r sums its share of the
+//     sources, and rank 0 adds the others' partial sums, read from their shared memory, in
+//     rank order -- deterministic, no workspace.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -53,6 +58,67 @@ __global__ void __launch_bounds__(kThreads, 2)
     block_points<ST, SUM, PAIRS>(sm, src, n, GRID, g, pts, m, first, field, out);
 }
 
+// Small launches: a cluster of S blocks per point tile, block rank r summing sources
+// [r c, (r + 1) c), c = ceil(n / S); rank 0 adds ranks 1 .. S-1's partial sums (read from their
+// shared memory through the cluster) in rank order, then stores.  Both cluster barriers are
+// reached by every thread of every block.
+template <int ST, int SUM, bool GRID, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_split_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                       const float* __restrict__ pts, int64_t m, int field,
+                       void* __restrict__ out) {
+    namespace cg = cooperative_groups;
+    __shared__ SmemTile sm;
+    constexpr int kPPT = 2 * PAIRS;
+    // partial sums (and compensations) of every thread, in the staging arrays once free
+    static_assert(sizeof(float2) * (SUM == SUM_COMPENSATED ? 2 : 1) * kPPT * kThreads <=
+                      4 * sizeof(sm.v0),
+                  "partial sums must fit in the first four staging arrays");
+    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned S = cluster.num_blocks();
+    const unsigned rank = cluster.block_rank();
+    const int64_t first = static_cast<int64_t>(blockIdx.x / S) * (kThreads * kPPT);
+    const int64_t chunk = (n + S - 1) / S;
+    const int64_t s_lo = static_cast<int64_t>(rank) * chunk < n ? static_cast<int64_t>(rank) * chunk : n;
+    const int64_t s_hi = s_lo + chunk < n ? s_lo + chunk : n;
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    block_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, GRID, g, pts, m, first, RE, IM, CRE,
+                                     CIM);
+    __syncthreads();  // the staging arrays are free
+    float2* part = reinterpret_cast<float2*>(sm.v0);
+#pragma unroll
+    for (int k = 0; k < kPPT; ++k) {
+        part[k * kThreads + threadIdx.x] =
+            make_float2(lane_of(RE[k >> 1], k & 1), lane_of(IM[k >> 1], k & 1));
+        if constexpr (SUM == SUM_COMPENSATED)
+            part[(kPPT + k) * kThreads + threadIdx.x] =
+                make_float2(lane_of(CRE[k >> 1], k & 1), lane_of(CIM[k >> 1], k & 1));
+    }
+    cluster.sync();
+    if (rank == 0) {
+        for (unsigned q = 1; q < S; ++q) {
+            const float2* rp = cluster.map_shared_rank(part, q);
+#pragma unroll
+            for (int k = 0; k < kPPT; ++k) {
+                const float2 v = rp[k * kThreads + threadIdx.x];
+                if constexpr (SUM == SUM_PLAIN) {
+                    lane_of(RE[k >> 1], k & 1) += v.x;
+                    lane_of(IM[k >> 1], k & 1) += v.y;
+                } else {
+                    const float2 c = rp[(kPPT + k) * kThreads + threadIdx.x];
+                    neumaier_add(lane_of(RE[k >> 1], k & 1), lane_of(CRE[k >> 1], k & 1), v.x);
+                    neumaier_add(lane_of(RE[k >> 1], k & 1), lane_of(CRE[k >> 1], k & 1), c.x);
+                    neumaier_add(lane_of(IM[k >> 1], k & 1), lane_of(CIM[k >> 1], k & 1), v.y);
+                    neumaier_add(lane_of(IM[k >> 1], k & 1), lane_of(CIM[k >> 1], k & 1), c.y);
+                }
+            }
+        }
+    }
+    cluster.sync();  // the other ranks' shared memory stays alive until rank 0 has read it
+    if (rank == 0) block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
+}
+
 // Grids with more than one point along their second axis: tiles of TX = 1 << tx_log2 first-axis
 // indices by (kThreads / TX) * 2 * PAIRS second-axis indices, one plane each (field_rows.cuh).
 template <int ST, int SUM, int PAIRS>
@@ -74,10 +140,47 @@ __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
 
 int g_num_sms = 0;
 
+// Cluster split of small launches: at most the portable cluster size, each block summing at
+// least kSplitMinSources sources.
+constexpr int64_t kMaxClusterBlocks = 8;
+constexpr int64_t kSplitMinSources = 64;
+
 template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
                          void* out, cudaStream_t s) {
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
+    const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
+    const int64_t want = 2LL * num_sms();
+    if (flat_blocks < want && n >= 2 * kSplitMinSources) {
+        // too few blocks to fill the GPU: split each tile's sources over a cluster
+        int64_t S = (want + flat_blocks - 1) / flat_blocks;
+        if (S > kMaxClusterBlocks) S = kMaxClusterBlocks;
+        if (S > n / kSplitMinSources) S = n / kSplitMinSources;
+        if (S >= 2) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(static_cast<unsigned>(flat_blocks * S), 1, 1);
+            cfg.blockDim = dim3(kThreads, 1, 1);
+            cfg.dynamicSmemBytes = 0;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = static_cast<unsigned>(S);
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            cudaError_t e;
+            if (ps.is_grid)
+                e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, true, PAIRS>, src, n,
+                                       ps.grid, static_cast<const float*>(nullptr), ps.m, field,
+                                       out);
+            else
+                e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, false, PAIRS>, src, n,
+                                       ps.grid, ps.pts, ps.m, field, out);
+            count_launch();
+            return e != cudaSuccess ? e : cudaGetLastError();
+        }
+    }
     if (ps.is_grid) {
         const RowsTiling t = rows_tiling(ps.grid, ps.m, PAIRS);
         if (t.use) {
@@ -88,7 +191,7 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
             return cudaGetLastError();
         }
     }
-    const int64_t blocks = (ps.m + per_block - 1) / per_block;
+    const int64_t blocks = flat_blocks;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     if (ps.is_grid) {
         field_direct_kernel<ST, SUM, true, PAIRS><<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(
