@@ -15,6 +15,11 @@ enum SolverKind : int { SOLVER_GSPAT = 0, SOLVER_GS = 1, SOLVER_NAIVE = 2, SOLVE
 // Largest candidate-phase count of the greedy solver (one thread per candidate).
 constexpr int kGreedyMaxDiv = 1024;
 
+// Nonlinear least-squares solvers (nls.cu) and their focus limit (their small dense systems
+// are 2m x 2m).
+enum NlsKind : int { NLS_GRADIENT_DESCENT = 0, NLS_GAUSS_NEWTON = 1, NLS_LM = 2 };
+constexpr int64_t kNlsMaxFoci = 256;
+
 // REPEAT of gs_pat.rs:17 and gs.rs:17.
 constexpr int kSolverRepeat = 100;
 // Largest focus count the single-block iteration kernels accept.
@@ -51,5 +56,11 @@ cudaError_t launch_greedy(int st, const float* d_raw, const float* d_k, const fl
 int solve_multi_focus(int kind, int st, float* src, const float* k, const float* atten,
                       int64_t n, const float* foci, const float* amps, int64_t m,
                       std::string* err, int phase_div = 0);
+
+// Gradient descent, Gauss-Newton or Levenberg-Marquardt phase retrieval
+// (multiple_foci/nls/*.rs) on the device; writes the phases into the host source array `src`
+// (ABI layout) in place, amplitudes unchanged.  Returns 0 on success, else fills *err.
+int solve_nls(int kind, int st, float* src, const float* k, const float* atten, int64_t n,
+              const float* foci, const float* amps, int64_t m, std::string* err);
 
 }  // namespace afc

@@ -447,6 +447,23 @@ void run_solver(int kind, void* handle, const void* foci, const float* amps, uin
     if (rc != 0) set_error("%s", err.c_str());
 }
 
+void run_nls(int kind, void* handle, const void* foci, const float* amps, uint64_t size,
+             int32_t st) {
+    if (!valid_source_type(st)) {
+        set_error("unknown source type %d", st);
+        return;
+    }
+    System* s = as_system(handle, st);
+    if (!s) return;
+    std::vector<float> f, a;
+    if (!unpack_foci(foci, amps, size, f, a)) return;
+    std::string err;
+    const int rc = solve_nls(kind, st, s->src.data(), s->k.data(), s->atten.data(),
+                             static_cast<int64_t>(s->count()), f.data(), a.data(),
+                             static_cast<int64_t>(size), &err);
+    if (rc != 0) set_error("%s", err.c_str());
+}
+
 void unsupported(const char* name) {
     set_error("%s: this solver is not provided by the GB300 library (system left unchanged)",
               name);
@@ -858,13 +875,18 @@ void AFO_IFFT(void*, const char*, AfcVector3, AfcVector3, AfcVector3, float, flo
 void AFO_Horn(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Horn"); }
 void AFO_Long(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Long"); }
 void AFO_APO(void*, const void*, const float*, uint64_t, float, int32_t) { unsupported("AFO_APO"); }
-void AFO_GaussNewton(void*, const void*, const float*, uint64_t, int32_t) {
-    unsupported("AFO_GaussNewton");
+void AFO_GaussNewton(void* handle, const void* foci, const float* amps, uint64_t size,
+                     int32_t source_type) {
+    run_nls(NLS_GAUSS_NEWTON, handle, foci, amps, size, source_type);
 }
-void AFO_GradientDescent(void*, const void*, const float*, uint64_t, int32_t) {
-    unsupported("AFO_GradientDescent");
+void AFO_GradientDescent(void* handle, const void* foci, const float* amps, uint64_t size,
+                         int32_t source_type) {
+    run_nls(NLS_GRADIENT_DESCENT, handle, foci, amps, size, source_type);
 }
-void AFO_LM(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_LM"); }
+void AFO_LM(void* handle, const void* foci, const float* amps, uint64_t size,
+            int32_t source_type) {
+    run_nls(NLS_LM, handle, foci, amps, size, source_type);
+}
 void AFO_Greedy(void* handle, const void* foci, const float* amps, uint64_t size,
                 uint64_t phase_div, int32_t source_type) {
     if (phase_div < 1 || phase_div > static_cast<uint64_t>(kGreedyMaxDiv)) {

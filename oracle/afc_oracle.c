@@ -471,6 +471,232 @@ ORC_EXPORT void oracle_greedy_f32(int st, float *src, const float *k, const floa
     free(tim);
 }
 
+/* ---------------------------------------------------------------- NLS phase retrieval
+ * nls/macros.rs:16-58 and nls/{gradient_descent,gauss_newton,lm}.rs in float64, with the
+ * reference's dense formulas taken literally: B = [G | -diag(amps)] (m x N, N = n + m, G with
+ * every phase 0), BhB = B^H B (N x N), T = exp(-i x): JtJ = Re(BhB o T T^H), Jtf = column sums of
+ * Im(BhB o T T^H); F(x) = Re(t^H BhB t), t = exp(i x).  Solves: (JtJ + mu I) by Cholesky (the
+ * reference's QR gives the same solution), pinv(JtJ, 1e-3) by a Jacobi eigendecomposition
+ * (JtJ is symmetric positive semi-definite, so its singular values are its eigenvalues).
+ * kind: 0 gradient descent, 1 Gauss-Newton, 2 Levenberg-Marquardt.  Writes the phases. */
+static void nls_jtj_jtf(const double *bre, const double *bim, int64_t N, const double *x,
+                        double *A, double *g) {
+    /* (BhB o T T^H)_ab = BhB_ab T_a conj(T_b), T = exp(-i x) */
+    for (int64_t b = 0; b < N; ++b) g[b] = 0.0;
+    for (int64_t a = 0; a < N; ++a)
+        for (int64_t b = 0; b < N; ++b) {
+            double hr = bre[a * N + b], hi = bim[a * N + b];
+            double ph = -x[a] + x[b]; /* T_a conj(T_b) = exp(-i x_a + i x_b) */
+            double cr = cos(ph), ci = sin(ph);
+            double vr = hr * cr - hi * ci, vi = hr * ci + hi * cr;
+            if (A) A[a * N + b] = vr;
+            g[b] += vi;
+        }
+}
+
+static double nls_fx(const double *bre, const double *bim, int64_t N, const double *x) {
+    double f = 0.0; /* Re(t^H BhB t), t = exp(i x) */
+    for (int64_t a = 0; a < N; ++a)
+        for (int64_t b = 0; b < N; ++b) {
+            double ph = -x[a] + x[b];
+            f += bre[a * N + b] * cos(ph) - bim[a * N + b] * sin(ph);
+        }
+    return f;
+}
+
+static int chol_solve(double *a, double *b, int64_t k) {
+    for (int64_t j = 0; j < k; ++j) {
+        double d = a[j * k + j];
+        for (int64_t p = 0; p < j; ++p) d -= a[j * k + p] * a[j * k + p];
+        if (!(d > 0.0)) return 0;
+        d = sqrt(d);
+        a[j * k + j] = d;
+        for (int64_t i = j + 1; i < k; ++i) {
+            double t = a[i * k + j];
+            for (int64_t p = 0; p < j; ++p) t -= a[i * k + p] * a[j * k + p];
+            a[i * k + j] = t / d;
+        }
+    }
+    for (int64_t i = 0; i < k; ++i) {
+        double t = b[i];
+        for (int64_t p = 0; p < i; ++p) t -= a[i * k + p] * b[p];
+        b[i] = t / a[i * k + i];
+    }
+    for (int64_t i = k - 1; i >= 0; --i) {
+        double t = b[i];
+        for (int64_t p = i + 1; p < k; ++p) t -= a[p * k + i] * b[p];
+        b[i] = t / a[i * k + i];
+    }
+    return 1;
+}
+
+/* Cyclic Jacobi: a (symmetric, destroyed) -> eigenvalues lam, eigenvectors in v's columns. */
+static void jacobi(double *a, int64_t k, double *lam, double *v) {
+    for (int64_t i = 0; i < k * k; ++i) v[i] = 0.0;
+    for (int64_t i = 0; i < k; ++i) v[i * k + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int64_t i = 0; i < k * k; ++i) tot += a[i] * a[i];
+        for (int64_t i = 0; i < k; ++i)
+            for (int64_t j = 0; j < k; ++j)
+                if (i != j) off += a[i * k + j] * a[i * k + j];
+        if (off <= 1e-30 * tot) break;
+        for (int64_t p = 0; p < k; ++p)
+            for (int64_t q = p + 1; q < k; ++q) {
+                double apq = a[p * k + q];
+                if (apq == 0.0) continue;
+                double th = (a[q * k + q] - a[p * k + p]) / (2.0 * apq);
+                double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int64_t r = 0; r < k; ++r) {
+                    double x1 = a[r * k + p], x2 = a[r * k + q];
+                    a[r * k + p] = c * x1 - sn * x2;
+                    a[r * k + q] = sn * x1 + c * x2;
+                }
+                for (int64_t r = 0; r < k; ++r) {
+                    double x1 = a[p * k + r], x2 = a[q * k + r];
+                    a[p * k + r] = c * x1 - sn * x2;
+                    a[q * k + r] = sn * x1 + c * x2;
+                }
+                for (int64_t r = 0; r < k; ++r) {
+                    double x1 = v[r * k + p], x2 = v[r * k + q];
+                    v[r * k + p] = c * x1 - sn * x2;
+                    v[r * k + q] = sn * x1 + c * x2;
+                }
+            }
+    }
+    for (int64_t i = 0; i < k; ++i) lam[i] = a[i * k + i];
+}
+
+static double vmax(const double *g, int64_t N) {
+    double mx = -INFINITY;
+    for (int64_t b = 0; b < N; ++b)
+        if (g[b] > mx) mx = g[b];
+    return mx;
+}
+
+static double vnorm(const double *v, int64_t N) {
+    double s2 = 0.0;
+    for (int64_t b = 0; b < N; ++b) s2 += v[b] * v[b];
+    return sqrt(s2);
+}
+
+ORC_EXPORT void oracle_nls_f64(int kind, int st, float *src, const float *k, const float *atten,
+                               int64_t n, const float *foci, const float *amps, int64_t m) {
+    const int stride = src_stride(st);
+    const int iphase = st == ORC_SRC_T4010A1 ? 7 : 4;
+    const int64_t N = n + m;
+    for (int64_t j = 0; j < n; ++j) src[stride * j + iphase] = 0.0f;
+    double *bre = calloc((size_t)(m * N + 1), sizeof(double));
+    double *bim = calloc((size_t)(m * N + 1), sizeof(double));
+    for (int64_t i = 0; i < m; ++i) {
+        for (int64_t j = 0; j < n; ++j)
+            prop_f64(st, src + stride * j, k[j], atten[j], foci[3 * i], foci[3 * i + 1],
+                     foci[3 * i + 2], &bre[i * N + j], &bim[i * N + j]);
+        bre[i * N + n + i] = -(double)amps[i];
+    }
+    double *hre = calloc((size_t)(N * N + 1), sizeof(double));
+    double *him = calloc((size_t)(N * N + 1), sizeof(double));
+    for (int64_t a = 0; a < N; ++a)
+        for (int64_t b = 0; b < N; ++b) {
+            double sr = 0, si = 0; /* sum_i conj(B_ia) B_ib */
+            for (int64_t i = 0; i < m; ++i) {
+                sr += bre[i * N + a] * bre[i * N + b] + bim[i * N + a] * bim[i * N + b];
+                si += bre[i * N + a] * bim[i * N + b] - bim[i * N + a] * bre[i * N + b];
+            }
+            hre[a * N + b] = sr;
+            him[a * N + b] = si;
+        }
+    double *x = calloc((size_t)(N + 1), sizeof(double));
+    double *g = calloc((size_t)(N + 1), sizeof(double));
+    double *h = calloc((size_t)(N + 1), sizeof(double));
+    double *xn = calloc((size_t)(N + 1), sizeof(double));
+    double *A = calloc((size_t)(N * N + 1), sizeof(double));
+    double *W = calloc((size_t)(N * N + 1), sizeof(double));
+    double *V = calloc((size_t)(N * N + 1), sizeof(double));
+    double *lam = calloc((size_t)(N + 1), sizeof(double));
+    if (kind == 0) { /* gradient_descent.rs:44-52 */
+        for (int it = 0; it < 10000; ++it) {
+            nls_jtj_jtf(hre, him, N, x, NULL, g);
+            if (vmax(g, N) <= 1e-6) break;
+            for (int64_t b = 0; b < N; ++b) x[b] -= 0.1 * g[b];
+        }
+    } else if (kind == 1) { /* gauss_newton.rs:44-85 */
+        nls_jtj_jtf(hre, him, N, x, A, g);
+        int found = vmax(g, N) <= 1e-8;
+        for (int it = 0; it < 200 && !found; ++it) {
+            memcpy(W, A, sizeof(double) * (size_t)(N * N));
+            jacobi(W, N, lam, V);
+            for (int64_t b = 0; b < N; ++b) h[b] = 0.0;
+            for (int64_t q = 0; q < N; ++q) {
+                if (!(lam[q] > 1e-3)) continue;
+                double proj = 0.0;
+                for (int64_t b = 0; b < N; ++b) proj += V[b * N + q] * g[b];
+                for (int64_t b = 0; b < N; ++b) h[b] -= V[b * N + q] * proj / lam[q];
+            }
+            if (vnorm(h, N) <= 1e-8 * (vnorm(x, N) + 1e-8)) {
+                found = 1;
+            } else {
+                for (int64_t b = 0; b < N; ++b) x[b] += h[b];
+                nls_jtj_jtf(hre, him, N, x, A, g);
+                found = vmax(g, N) <= 1e-8;
+            }
+        }
+    } else { /* lm.rs:44-100 */
+        double nu = 2.0;
+        nls_jtj_jtf(hre, him, N, x, A, g);
+        double a_max = -INFINITY;
+        for (int64_t b = 0; b < N; ++b)
+            if (A[b * N + b] > a_max) a_max = A[b * N + b];
+        double mu = 1e-3 * a_max;
+        int found = vmax(g, N) <= 1e-8;
+        double fx = nls_fx(hre, him, N, x);
+        for (int it = 0; it < 200 && !found; ++it) {
+            memcpy(W, A, sizeof(double) * (size_t)(N * N));
+            for (int64_t b = 0; b < N; ++b) W[b * N + b] += mu;
+            for (int64_t b = 0; b < N; ++b) h[b] = g[b];
+            if (!chol_solve(W, h, N)) break;
+            for (int64_t b = 0; b < N; ++b) h[b] = -h[b];
+            if (vnorm(h, N) <= 1e-8 * (vnorm(x, N) + 1e-8)) {
+                found = 1;
+            } else {
+                for (int64_t b = 0; b < N; ++b) xn[b] = x[b] + h[b];
+                double fx_new = nls_fx(hre, him, N, xn);
+                double l0 = 0.0;
+                for (int64_t b = 0; b < N; ++b) l0 += h[b] * (mu * h[b] - g[b]);
+                l0 *= 0.5;
+                double rho = (fx - fx_new) / l0;
+                fx = fx_new;
+                if (rho > 0.0) {
+                    memcpy(x, xn, sizeof(double) * (size_t)N);
+                    nls_jtj_jtf(hre, him, N, x, A, g);
+                    found = vmax(g, N) <= 1e-8;
+                    double c = 2.0 * rho - 1.0;
+                    double f = 1.0 - c * c * c;
+                    mu *= f > 1.0 / 3.0 ? f : 1.0 / 3.0;
+                    nu = 2.0;
+                } else {
+                    mu *= nu;
+                    nu *= 2.0;
+                }
+            }
+        }
+    }
+    for (int64_t j = 0; j < n; ++j) src[stride * j + iphase] = (float)x[j];
+    free(bre);
+    free(bim);
+    free(hre);
+    free(him);
+    free(x);
+    free(g);
+    free(h);
+    free(xn);
+    free(A);
+    free(W);
+    free(V);
+    free(lam);
+}
+
 /* ---------------------------------------------------------------- G and the solvers */
 
 /* macros.rs:32-53: G[i, j] = propagate(source j, focus i) with the sources' current amp and

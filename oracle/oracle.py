@@ -65,6 +65,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_focal_point.argtypes = [c_int, fp, c_int64, c_float, c_float, c_float, c_float]
         L.oracle_bessel_beam.argtypes = [c_int, fp, c_int64, c_float] + [c_float] * 7
         L.oracle_greedy_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int]
+        L.oracle_nls_f64.argtypes = [c_int, c_int, fp, fp, fp, c_int64, fp, fp, c_int64]
         L.oracle_build_g_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, fp]
         L.oracle_build_g_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, dp, c_int]
         L.oracle_gspat_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int, dp]
@@ -221,6 +222,22 @@ def greedy_f32(st, sources, k, atten, foci, amps, phase_div=16) -> np.ndarray:
     amps = np.ascontiguousarray(amps, dtype=np.float32)
     lib().oracle_greedy_f32(st, _f(s), _f(k), _f(atten), len(k), _f(foci), _f(amps), len(amps),
                             int(phase_div))
+    return s
+
+
+NLS_GRADIENT_DESCENT, NLS_GAUSS_NEWTON, NLS_LM = 0, 1, 2
+
+
+def nls_f64(kind, st, sources, k, atten, foci, amps) -> np.ndarray:
+    """Sources with the phases of gradient descent / Gauss-Newton / LM (nls/*.rs, float64,
+    dense formulas)."""
+    s = np.array(sources, dtype=np.float32, copy=True).reshape(-1)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    atten = np.ascontiguousarray(atten, dtype=np.float32)
+    foci = np.ascontiguousarray(foci, dtype=np.float32).reshape(-1, 3)
+    amps = np.ascontiguousarray(amps, dtype=np.float32)
+    lib().oracle_nls_f64(kind, st, _f(s), _f(k), _f(atten), len(k), _f(foci), _f(amps),
+                         len(amps))
     return s
 
 
