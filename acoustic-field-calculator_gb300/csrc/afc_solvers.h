@@ -63,4 +63,9 @@ int solve_multi_focus(int kind, int st, float* src, const float* k, const float*
 int solve_nls(int kind, int st, float* src, const float* k, const float* atten, int64_t n,
               const float* foci, const float* amps, int64_t m, std::string* err);
 
+// Acoustic power optimization (multiple_foci/nls/apo.rs) on the device, regularisation lambda;
+// writes amplitudes and phases into `src` in place.  n <= 65535 (its n x n matrix).
+int solve_apo(int st, float* src, const float* k, const float* atten, int64_t n,
+              const float* foci, const float* amps, int64_t m, float lambda, std::string* err);
+
 }  // namespace afc

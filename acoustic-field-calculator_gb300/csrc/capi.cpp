@@ -874,7 +874,22 @@ void AFO_IFFT(void*, const char*, AfcVector3, AfcVector3, AfcVector3, float, flo
 }
 void AFO_Horn(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Horn"); }
 void AFO_Long(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Long"); }
-void AFO_APO(void*, const void*, const float*, uint64_t, float, int32_t) { unsupported("AFO_APO"); }
+void AFO_APO(void* handle, const void* foci, const float* amps, uint64_t size, float lambda,
+             int32_t source_type) {
+    if (!valid_source_type(source_type)) {
+        set_error("unknown source type %d", source_type);
+        return;
+    }
+    System* s = as_system(handle, source_type);
+    if (!s) return;
+    std::vector<float> f, a;
+    if (!unpack_foci(foci, amps, size, f, a)) return;
+    std::string err;
+    const int rc = solve_apo(source_type, s->src.data(), s->k.data(), s->atten.data(),
+                             static_cast<int64_t>(s->count()), f.data(), a.data(),
+                             static_cast<int64_t>(size), lambda, &err);
+    if (rc != 0) set_error("%s", err.c_str());
+}
 void AFO_GaussNewton(void* handle, const void* foci, const float* amps, uint64_t size,
                      int32_t source_type) {
     run_nls(NLS_GAUSS_NEWTON, handle, foci, amps, size, source_type);

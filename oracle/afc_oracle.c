@@ -697,6 +697,168 @@ ORC_EXPORT void oracle_nls_f64(int kind, int st, float *src, const float *k, con
     free(lam);
 }
 
+/* ---------------------------------------------------------------- APO
+ * nls/apo.rs:36-158 in float64, literally: explicit R_i = G^H D_i G (n x n each),
+ * q0 = (G^H G + lambda I)^-1 G^H p (Cholesky; the reference's QR gives the same solution),
+ * J(q) = sum_i |q^H R_i q - p_i^2|^2 + lambda |q.q| (nalgebra's dot: no conjugation),
+ * grad J = sum_i R_i q (p_i^2 - |q^H R_i q|) + lambda q, the line search over a = i / 100,
+ * and H += y y^T / (y.s) - (H s)(H s)^T / (s^T H s) (transposes, bilinear dots).  The output
+ * amplitude is amp |q_j| / camax(q), camax being nalgebra 0.27.1's largest |re| + |im| of the
+ * entries; the phase is arg q_j. */
+#include <complex.h>
+
+static double apo_J(const double complex *R, const double complex *q, const double *p2, int64_t n,
+                    int64_t m, double lambda) {
+    double v = 0.0;
+    for (int64_t i = 0; i < m; ++i) {
+        double complex qrq = 0.0;
+        for (int64_t a = 0; a < n; ++a) {
+            double complex rq = 0.0;
+            for (int64_t b = 0; b < n; ++b) rq += R[(i * n + a) * n + b] * q[b];
+            qrq += conj(q[a]) * rq;
+        }
+        double complex t = qrq - p2[i];
+        v += creal(t) * creal(t) + cimag(t) * cimag(t);
+    }
+    double complex qq = 0.0;
+    for (int64_t b = 0; b < n; ++b) qq += q[b] * q[b];
+    return v + cabs(qq) * lambda;
+}
+
+static void apo_grad(const double complex *R, const double complex *q, const double *p2,
+                     int64_t n, int64_t m, double lambda, double complex *g) {
+    for (int64_t a = 0; a < n; ++a) g[a] = lambda * q[a];
+    for (int64_t i = 0; i < m; ++i) {
+        double complex qrq = 0.0;
+        for (int64_t a = 0; a < n; ++a) {
+            double complex rq = 0.0;
+            for (int64_t b = 0; b < n; ++b) rq += R[(i * n + a) * n + b] * q[b];
+            qrq += conj(q[a]) * rq;
+        }
+        double s = p2[i] - cabs(qrq);
+        for (int64_t a = 0; a < n; ++a) {
+            double complex rq = 0.0;
+            for (int64_t b = 0; b < n; ++b) rq += R[(i * n + a) * n + b] * q[b];
+            g[a] += rq * s;
+        }
+    }
+}
+
+ORC_EXPORT void oracle_apo_f64(int st, float *src, const float *k, const float *atten, int64_t n,
+                               const float *foci, const float *amps, int64_t m, float lambda) {
+    const int stride = src_stride(st);
+    const int iamp = st == ORC_SRC_T4010A1 ? 6 : 3;
+    const int iphase = st == ORC_SRC_T4010A1 ? 7 : 4;
+    for (int64_t j = 0; j < n; ++j) src[stride * j + iphase] = 0.0f;
+    double complex *G = calloc((size_t)(m * n + 1), sizeof(double complex));
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t j = 0; j < n; ++j) {
+            double re, im;
+            prop_f64(st, src + stride * j, k[j], atten[j], foci[3 * i], foci[3 * i + 1],
+                     foci[3 * i + 2], &re, &im);
+            G[i * n + j] = re + I * im;
+        }
+    double *p2 = calloc((size_t)(m + 1), sizeof(double));
+    for (int64_t i = 0; i < m; ++i) p2[i] = (double)amps[i] * (double)amps[i];
+    /* q0: (G^H G + lambda I) q0 = G^H p, complex Cholesky */
+    double complex *A = calloc((size_t)(n * n + 1), sizeof(double complex));
+    double complex *q = calloc((size_t)(n + 1), sizeof(double complex));
+    for (int64_t a = 0; a < n; ++a) {
+        for (int64_t b = 0; b < n; ++b) {
+            double complex v = 0.0;
+            for (int64_t i = 0; i < m; ++i) v += conj(G[i * n + a]) * G[i * n + b];
+            A[a * n + b] = v + (a == b ? (double)lambda : 0.0);
+        }
+        double complex v = 0.0;
+        for (int64_t i = 0; i < m; ++i) v += conj(G[i * n + a]) * (double)amps[i];
+        q[a] = v;
+    }
+    for (int64_t j = 0; j < n; ++j) { /* A = L L^H in place (lower) */
+        double d = creal(A[j * n + j]);
+        for (int64_t p = 0; p < j; ++p) d -= creal(A[j * n + p] * conj(A[j * n + p]));
+        d = sqrt(d);
+        A[j * n + j] = d;
+        for (int64_t i = j + 1; i < n; ++i) {
+            double complex t = A[i * n + j];
+            for (int64_t p = 0; p < j; ++p) t -= A[i * n + p] * conj(A[j * n + p]);
+            A[i * n + j] = t / d;
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        double complex t = q[i];
+        for (int64_t p = 0; p < i; ++p) t -= A[i * n + p] * q[p];
+        q[i] = t / creal(A[i * n + i]);
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+        double complex t = q[i];
+        for (int64_t p = i + 1; p < n; ++p) t -= conj(A[p * n + i]) * q[p];
+        q[i] = t / creal(A[i * n + i]);
+    }
+    double complex *R = calloc((size_t)(m * n * n + 1), sizeof(double complex));
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t a = 0; a < n; ++a)
+            for (int64_t b = 0; b < n; ++b) R[(i * n + a) * n + b] = conj(G[i * n + a]) * G[i * n + b];
+    double complex *H = calloc((size_t)(n * n + 1), sizeof(double complex));
+    for (int64_t a = 0; a < n; ++a) H[a * n + a] = 1.0;
+    double complex *g = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *gn = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *d = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *qn = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *sv = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *u = calloc((size_t)(n + 1), sizeof(double complex));
+    double complex *tmp = calloc((size_t)(n + 1), sizeof(double complex));
+    apo_grad(R, q, p2, n, m, lambda, g);
+    for (int it = 0; it < 200; ++it) {
+        for (int64_t a = 0; a < n; ++a) {
+            double complex v = 0.0;
+            for (int64_t b = 0; b < n; ++b) v += H[a * n + b] * g[b];
+            d[a] = -v;
+        }
+        double alpha = 0.0, best = INFINITY;
+        for (int li = 0; li < 100; ++li) {
+            double a = (double)((float)li / 100.0f);
+            for (int64_t b = 0; b < n; ++b) tmp[b] = q[b] + d[b] * a;
+            double v = apo_J(R, tmp, p2, n, m, lambda);
+            if (v < best) {
+                best = v;
+                alpha = a;
+            }
+        }
+        double dn = 0.0;
+        for (int64_t b = 0; b < n; ++b) {
+            d[b] *= alpha;
+            dn += creal(d[b] * conj(d[b]));
+        }
+        if (sqrt(dn) < 1e-8) break;
+        for (int64_t b = 0; b < n; ++b) qn[b] = q[b] + d[b];
+        apo_grad(R, qn, p2, n, m, lambda, gn);
+        for (int64_t b = 0; b < n; ++b) sv[b] = gn[b] - g[b];
+        double complex ys = 0.0, su = 0.0;
+        for (int64_t a = 0; a < n; ++a) {
+            double complex v = 0.0;
+            for (int64_t b = 0; b < n; ++b) v += H[a * n + b] * sv[b];
+            u[a] = v;
+        }
+        for (int64_t b = 0; b < n; ++b) {
+            ys += d[b] * sv[b];
+            su += sv[b] * u[b];
+        }
+        for (int64_t a = 0; a < n; ++a)
+            for (int64_t b = 0; b < n; ++b) H[a * n + b] += d[a] * d[b] / ys - u[a] * u[b] / su;
+        memcpy(q, qn, sizeof(double complex) * (size_t)n);
+        memcpy(g, gn, sizeof(double complex) * (size_t)n);
+    }
+    double mx = 0.0; /* nalgebra 0.27.1 camax: the largest |re| + |im| */
+    for (int64_t b = 0; b < n; ++b)
+        if (fabs(creal(q[b])) + fabs(cimag(q[b])) > mx) mx = fabs(creal(q[b])) + fabs(cimag(q[b]));
+    for (int64_t b = 0; b < n; ++b) {
+        src[stride * b + iamp] = (float)((double)src[stride * b + iamp] * cabs(q[b]) / mx);
+        src[stride * b + iphase] = (float)carg(q[b]);
+    }
+    free(G); free(p2); free(A); free(q); free(R); free(H); free(g); free(gn); free(d); free(qn);
+    free(sv); free(u); free(tmp);
+}
+
 /* ---------------------------------------------------------------- G and the solvers */
 
 /* macros.rs:32-53: G[i, j] = propagate(source j, focus i) with the sources' current amp and

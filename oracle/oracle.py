@@ -66,6 +66,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_bessel_beam.argtypes = [c_int, fp, c_int64, c_float] + [c_float] * 7
         L.oracle_greedy_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int]
         L.oracle_nls_f64.argtypes = [c_int, c_int, fp, fp, fp, c_int64, fp, fp, c_int64]
+        L.oracle_apo_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_float]
         L.oracle_build_g_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, fp]
         L.oracle_build_g_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, dp, c_int]
         L.oracle_gspat_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int, dp]
@@ -238,6 +239,18 @@ def nls_f64(kind, st, sources, k, atten, foci, amps) -> np.ndarray:
     amps = np.ascontiguousarray(amps, dtype=np.float32)
     lib().oracle_nls_f64(kind, st, _f(s), _f(k), _f(atten), len(k), _f(foci), _f(amps),
                          len(amps))
+    return s
+
+
+def apo_f64(st, sources, k, atten, foci, amps, lambda_reg) -> np.ndarray:
+    """Sources with APO's amplitudes and phases (nls/apo.rs, float64, dense R_i)."""
+    s = np.array(sources, dtype=np.float32, copy=True).reshape(-1)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    atten = np.ascontiguousarray(atten, dtype=np.float32)
+    foci = np.ascontiguousarray(foci, dtype=np.float32).reshape(-1, 3)
+    amps = np.ascontiguousarray(amps, dtype=np.float32)
+    lib().oracle_apo_f64(st, _f(s), _f(k), _f(atten), len(k), _f(foci), _f(amps), len(amps),
+                         float(lambda_reg))
     return s
 
 
