@@ -36,7 +36,8 @@ def _cuda_home() -> str:
 def _sources():
     cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+               if f.endswith((".h", ".cuh", ".inc"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     return cu, cpp, headers
 

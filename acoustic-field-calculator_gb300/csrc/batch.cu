@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                  unsigned long long* __restrict__ counter, const PackedSource* __restrict__ arena) {
     __shared__ SmemTile sm;
     __shared__ long long s_item;
-    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table_b[threadIdx.x];
+    load_dir_tables(sm, c_dir_table_b);
     for (;;) {
         __syncthreads();  // the previous item's readers of sm and s_item are done
         if (threadIdx.x == 0) s_item = static_cast<long long>(atomicAdd(counter, 1ull));

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                         const float* __restrict__ pts, int64_t m, int field,
                         void* __restrict__ out) {
     __shared__ SmemTile sm;
-    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
+    load_dir_tables(sm, c_dir_table);
     const int64_t first = static_cast<int64_t>(blockIdx.x) * (kThreads * 2 * PAIRS);
     block_points<ST, SUM, PAIRS>(sm, src, n, GRID, g, pts, m, first, field, out);
 }
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     static_assert(sizeof(float2) * (SUM == SUM_COMPENSATED ? 2 : 1) * kPPT * kThreads <=
                       4 * sizeof(sm.v0),
                   "partial sums must fit in the first four staging arrays");
-    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
+    load_dir_tables(sm, c_dir_table);
     cg::cluster_group cluster = cg::this_cluster();
     const unsigned S = cluster.num_blocks();
     const unsigned rank = cluster.block_rank();
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     field_rows_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g, int tx_log2,
                       int64_t tiles0, int64_t tiles1, int field, void* __restrict__ out) {
     __shared__ SmemTile sm;
-    if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = c_dir_table[threadIdx.x];
+    load_dir_tables(sm, c_dir_table);
     block_rows<ST, SUM, PAIRS>(sm, src, n, g, tx_log2, tiles0, tiles1, blockIdx.x, field, out);
 }
 

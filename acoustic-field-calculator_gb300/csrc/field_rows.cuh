@@ -54,16 +54,19 @@ struct RowGeom {
 // recomputed from the offsets as the hot loop computed it; the reference's bin needs the
 // offsets and the direction back in x, y, z order (a0, a1, a2: the xyz index of each grid
 // axis).
-static __device__ __noinline__ float2 edge_correction_rows(const float4* __restrict__ tab, float du,
-                                                    float dv, float dw, float vw2, float cn,
-                                                    float n_a0, float n_a1, float n_a2, int a0,
-                                                    int a1, float k, float phase, float a2c,
-                                                    float la) {
+static __device__ __noinline__ float2 edge_correction_rows(const float4* __restrict__ tab,
+                                                           const float* __restrict__ cneg,
+                                                           const float4* __restrict__ ccoef,
+                                                           float du, float dv, float dw, float vw2,
+                                                           float cn, float n_a0, float n_a1,
+                                                           float n_a2, int a0, int a1, float k,
+                                                           float phase, float a2c, float la) {
     const float r2 = fmaf(du, du, vw2);
     const float rinv = mufu_rsqrt(r2);
     const float ct = cn * rinv;
+    float2 t;
+    const float d_fast = directivity2_ctab(cneg, ccoef, make_float2(ct, ct), t).x;
     const float thc = theta2_centred(make_float2(ct, ct)).x;
-    const int i_fast = fast_bin(thc);
     // back to x, y, z: the first grid axis carries v, the second u, the third w
     const float dx = a0 == 0 ? dv : (a1 == 0 ? du : dw);
     const float dy = a0 == 1 ? dv : (a1 == 1 ? du : dw);
@@ -72,11 +75,10 @@ static __device__ __noinline__ float2 edge_correction_rows(const float4* __restr
     const float ny = a0 == 1 ? n_a0 : (a1 == 1 ? n_a1 : n_a2);
     const float nz = a0 == 2 ? n_a0 : (a1 == 2 ? n_a1 : n_a2);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
-    if (i_exact == i_fast) return make_float2(0.f, 0.f);
     const float r = r2 * rinv;
     const float w0 = rinv * mufu_ex2(fmaf(a2c, r, la));
     const float red = reduce_phase2(f2(k), f2(r), f2(phase)).x;
-    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - dir_in_bin(tab, thc, i_fast));
+    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - d_fast);
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 
@@ -112,9 +114,9 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
-            float2 xc;
-            w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
-            any_near |= near_edge(xc.x) | near_edge(xc.y);
+            float2 t;
+            w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
+            any_near |= near_edge_c(t.x) | near_edge_c(t.y);
         }
         const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -137,13 +139,13 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
 #pragma unroll
             for (int q = 0; q < PAIRS; ++q) {
                 const RowGeom<UD> p(U[q], NP[q], sh, v0, v2, ns);
-                float2 xc;
-                directivity2_fast(sm.dir, p.ct, xc);
+                float2 t;
+                directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    if (!near_edge(lane_of(xc, h))) continue;
+                    if (!near_edge_c(lane_of(t, h))) continue;
                     const float2 c = edge_correction_rows(
-                        sm.dir, lane_of(p.du, h), sh.dv, sh.dw, sh.vw2, lane_of(p.cn, h), n_a0,
+                        sm.dir, sm.cneg, sm.ccoef, lane_of(p.du, h), sh.dv, sh.dw, sh.vw2, lane_of(p.cn, h), n_a0,
                         n_a1, n_a2, a0, a1, v1.z, v4.z, v3.z, v4.x);
                     if constexpr (SUM == SUM_PLAIN) {
                         lane_of(RE[q], h) += c.x;

@@ -234,6 +234,47 @@ __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ t
 
 __device__ __forceinline__ bool near_edge(float xc) { return fabsf(xc) > kEdgeBound; }
 
+// ------------------------------------------------------------------ directivity from cos(theta)
+//
+// The hot loops take D as a function of c = cos(theta) directly, without theta = acos(c) and
+// its MUFU square root: [-1/K, 1 + 1/K) is cut into intervals of width 1/K, and interval i
+// (c in [(i - 1)/K, i/K)) holds a cubic in x = c K - (i - 1) for each side of the bin edge it
+// may contain (dir_ctable.py derives the table, within 1.3e-7 of D(acos c) in float32).  The
+// side is the sign of c - L, L the edge's threshold on c; a pair within kCTabMargin of L (above
+// the fast c's error, a few 1e-7) is recomputed by the kernels' exact edge path.  c below -1/K
+// is clamped to -1/K, whose lower side is bin 10 (D = 0); c in [1, 2) (a unit cosine rounded
+// up, or a direction longer than 1, where the reference's acos is NaN and its bin 0) gives 1.
+// The index is masked, so it stays inside the table for every c, NaN and infinities included
+// (fmaxf returns -1/K for NaN); only a direction longer than 2 can land on a wrong entry.
+#include "dir_ctable.inc"
+
+constexpr int kCTabK = AFC_CTAB_K;
+constexpr int kCTabSize = AFC_CTAB_SIZE;
+constexpr float kCTabMagic = 8388609.0f;  // 2^23 + 1: RD(c K + 2^23 + 1) = 2^23 + 1 + floor(c K)
+constexpr float kCTabMargin = 4.0e-6f;
+static_assert((kCTabSize & (kCTabSize - 1)) == 0 && kCTabSize >= kCTabK + 2, "table index mask");
+
+// D of two points from their fast cos(theta).  negedge[i] = -L of interval i (-1e30 without an
+// edge), coef[2 i + side] the cubic of its side; t receives c - L.
+__device__ __forceinline__ float2 directivity2_ctab(const float* __restrict__ negedge,
+                                                    const float4* __restrict__ coef, float2 ct,
+                                                    float2& t) {
+    const float lo = -1.0f / static_cast<float>(kCTabK);
+    const float2 cc = make_float2(fmaxf(ct.x, lo), fmaxf(ct.y, lo));
+    const float2 fq = __ffma2_rd(cc, f2(static_cast<float>(kCTabK)), f2(kCTabMagic));
+    const float2 nfi = fma2(fq, f2(-1.0f), f2(kCTabMagic));          // -floor(c K)
+    const float2 x = fma2(cc, f2(static_cast<float>(kCTabK)), nfi);  // c K - floor(c K), exact
+    const int ix = __float_as_int(fq.x) & (kCTabSize - 1);
+    const int iy = __float_as_int(fq.y) & (kCTabSize - 1);
+    t = add2(ct, make_float2(negedge[ix], negedge[iy]));
+    const float4 a = coef[(ix << 1) | static_cast<int>(__float_as_uint(t.x) >> 31)];
+    const float4 b = coef[(iy << 1) | static_cast<int>(__float_as_uint(t.y) >> 31)];
+    return make_float2(fmaf(fmaf(fmaf(a.w, x.x, a.z), x.x, a.y), x.x, a.x),
+                       fmaf(fmaf(fmaf(b.w, x.y, b.z), x.y, b.y), x.y, b.x));
+}
+
+__device__ __forceinline__ bool near_edge_c(float t) { return fabsf(t) < kCTabMargin; }
+
 // Directivity of two points with the exact path applied in place (used where the pair is not
 // on the hot loop).
 __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, float2 ct, float2 dx,
