@@ -201,7 +201,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         if constexpr (UD) ns = sm.ns[j];
         else v2 = sm.v2[j];
     }
-    bool any_near = false;
+    float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
@@ -211,7 +211,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         if constexpr (ST == SRC_T4010A1) {
             float2 t;
             w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
-            any_near |= near_edge_c(t.x) | near_edge_c(t.y);
+            near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
         }
         const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -228,7 +228,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         }
     }
     if constexpr (ST == SRC_T4010A1) {
-        if (any_near) {
+        if (near_min < kCTabMargin) {
 #pragma unroll
             for (int k = 0; k < 2 * PAIRS; ++k) {
                 const int q = k >> 1, h = k & 1;

@@ -106,7 +106,7 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
     sh.vw2 = fmaf(sh.dw, sh.dw, sh.dv * sh.dv);
     sh.nvw = 0.f;
     if constexpr (ST == SRC_T4010A1 && !UD) sh.nvw = fmaf(v3.x, sh.dw, v2.x * sh.dv);
-    bool any_near = false;
+    float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const RowGeom<UD> p(U[q], NP[q], sh, v0, v2, ns);
@@ -116,7 +116,7 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
         if constexpr (ST == SRC_T4010A1) {
             float2 t;
             w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
-            any_near |= near_edge_c(t.x) | near_edge_c(t.y);
+            near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
         }
         const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -133,7 +133,7 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
         }
     }
     if constexpr (ST == SRC_T4010A1) {
-        if (any_near) {
+        if (near_min < kCTabMargin) {
             const float n_a0 = UD ? n0a.x : v2.x, n_a1 = UD ? n0a.y : v2.z,
                         n_a2 = UD ? n0a.z : v3.x;
 #pragma unroll

@@ -237,33 +237,33 @@ __device__ __forceinline__ bool near_edge(float xc) { return fabsf(xc) > kEdgeBo
 // ------------------------------------------------------------------ directivity from cos(theta)
 //
 // The hot loops take D as a function of c = cos(theta) directly, without theta = acos(c) and
-// its MUFU square root: [-1/K, 1 + 1/K) is cut into intervals of width 1/K, and interval i
-// (c in [(i - 1)/K, i/K)) holds a cubic in x = c K - (i - 1) for each side of the bin edge it
+// its MUFU square root: the c axis is cut into intervals of width 1/K, and interval
+// i = floor(c K) + BIAS holds a cubic in x = c K - floor(c K) for each side of the bin edge it
 // may contain (dir_ctable.py derives the table, within 1.3e-7 of D(acos c) in float32).  The
 // side is the sign of c - L, L the edge's threshold on c; a pair within kCTabMargin of L (above
-// the fast c's error, a few 1e-7) is recomputed by the kernels' exact edge path.  c below -1/K
-// is clamped to -1/K, whose lower side is bin 10 (D = 0); c in [1, 2) (a unit cosine rounded
-// up, or a direction longer than 1, where the reference's acos is NaN and its bin 0) gives 1.
-// The index is masked, so it stays inside the table for every c, NaN and infinities included
-// (fmaxf returns -1/K for NaN); only a direction longer than 2 can land on a wrong entry.
+// the fast c's error, a few 1e-7) is recomputed by the kernels' exact edge path.  Intervals
+// below -1/K give 0 (bin 10); c in [1, 3) (a unit cosine rounded up, or a direction longer than
+// 1, where the reference's acos is NaN and its bin 0) gives 1.  The index is masked, so it
+// stays inside the table for every c, NaN and infinities included; only a direction longer
+// than 3 can land on a wrong entry.
 #include "dir_ctable.inc"
 
 constexpr int kCTabK = AFC_CTAB_K;
 constexpr int kCTabSize = AFC_CTAB_SIZE;
-constexpr float kCTabMagic = 8388609.0f;  // 2^23 + 1: RD(c K + 2^23 + 1) = 2^23 + 1 + floor(c K)
+// RD(c K + 2^23 + BIAS) = 2^23 + BIAS + floor(c K) for every c >= -BIAS / K (> -1)
+constexpr float kCTabMagic = 8388608.0f + AFC_CTAB_BIAS;
 constexpr float kCTabMargin = 4.0e-6f;
-static_assert((kCTabSize & (kCTabSize - 1)) == 0 && kCTabSize >= kCTabK + 2, "table index mask");
+static_assert((kCTabSize & (kCTabSize - 1)) == 0 && kCTabSize >= AFC_CTAB_BIAS + 2 * kCTabK,
+              "table index mask");
 
 // D of two points from their fast cos(theta).  negedge[i] = -L of interval i (-1e30 without an
 // edge), coef[2 i + side] the cubic of its side; t receives c - L.
 __device__ __forceinline__ float2 directivity2_ctab(const float* __restrict__ negedge,
                                                     const float4* __restrict__ coef, float2 ct,
                                                     float2& t) {
-    const float lo = -1.0f / static_cast<float>(kCTabK);
-    const float2 cc = make_float2(fmaxf(ct.x, lo), fmaxf(ct.y, lo));
-    const float2 fq = __ffma2_rd(cc, f2(static_cast<float>(kCTabK)), f2(kCTabMagic));
+    const float2 fq = __ffma2_rd(ct, f2(static_cast<float>(kCTabK)), f2(kCTabMagic));
     const float2 nfi = fma2(fq, f2(-1.0f), f2(kCTabMagic));          // -floor(c K)
-    const float2 x = fma2(cc, f2(static_cast<float>(kCTabK)), nfi);  // c K - floor(c K), exact
+    const float2 x = fma2(ct, f2(static_cast<float>(kCTabK)), nfi);  // c K - floor(c K), exact
     const int ix = __float_as_int(fq.x) & (kCTabSize - 1);
     const int iy = __float_as_int(fq.y) & (kCTabSize - 1);
     t = add2(ct, make_float2(negedge[ix], negedge[iy]));

@@ -42,8 +42,8 @@ def test_edges_sit_in_the_interval_the_kernel_indexes():
     ths = BE.thresholds()
     for b in range(3, 11):
         e = np.float32(ths[b - 1])
-        # the kernels' index: RD(c K + 2^23 + 1) & (SIZE - 1), c clamped to -1/K
-        i = (int(np.floor(np.float64(e) * CT.K)) + 1) & (CT.SIZE - 1)
+        # the kernels' index: RD(c K + 2^23 + BIAS) & (SIZE - 1)
+        i = (int(np.floor(np.float64(e) * CT.K)) + CT.BIAS) & (CT.SIZE - 1)
         assert ne[i] == -e
         assert bins[2 * i] == b - 1 and bins[2 * i + 1] == b
     assert np.count_nonzero(ne != np.float32(-CT.NO_EDGE)) == 8
