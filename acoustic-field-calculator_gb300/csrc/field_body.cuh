@@ -51,9 +51,9 @@ __device__ __forceinline__ PackedSource pack_source(int st, const float* __restr
 struct SmemTile {
     float4 v0[kTile], v1[kTile], v2[kTile], v3[kTile], v4[kTile];
     float2 ns[kTile];
-    float4 dir[kDirTableSize];          // theta-binned cubics (the exact edge path)
-    float cneg[kCTabSize];              // cos(theta)-indexed table: -L per interval
-    float4 ccoef[2 * kCTabSize];        // and the cubic of each side
+    float4 dir[kDirTableSize];    // theta-binned cubics (this body; the exact edge paths)
+    float cneg[kCTabSize];        // cos(theta)-indexed table of the rows body: -L per interval
+    float4 ccoef[2 * kCTabSize];  // and the cubic of each side
     float box[kThreads / 32][6];  // per-warp bounds of the block's points (min xyz, max xyz)
     float bbox[6];                // the block's bounds
 };
@@ -129,17 +129,13 @@ __device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase
 
 // Correction for one point of a thread whose points include one next to a bin edge: recompute
 // the pair with the hot loop's operations (UD: cos(theta) from the shared direction); if its
-// fast cos(theta) is next to an edge of the cos(theta)-indexed table, return
-// w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators, else zero.
-// D_exact is the cubic of the reference's bin (exact_bin) at the fast theta.  Everything passes
-// by value so that the caller's accumulators stay in registers.
+// fast theta is next to an edge and the reference's bin (exact_bin) differs from the fast one,
+// return w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators, else
+// zero.  Everything passes by value so that the caller's accumulators stay in registers.
 template <bool UD>
-__device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab,
-                                               const float* __restrict__ cneg,
-                                               const float4* __restrict__ ccoef, float4 v0,
-                                               float4 v1, float4 v2, float4 v3, float4 v4,
-                                               float2 ns, float3 n0, float np, float px, float py,
-                                               float pz) {
+__device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
+                                               float4 v2, float4 v3, float4 v4, float2 ns,
+                                               float3 n0, float np, float px, float py, float pz) {
     const float dx = px + v0.x, dy = py + v0.z, dz = pz + v1.x;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float rinv = mufu_rsqrt(r2);
@@ -155,15 +151,17 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab,
         ny = v2.z;
         nz = v3.x;
     }
-    float2 t;
-    const float d_fast = directivity2_ctab(cneg, ccoef, make_float2(ct, ct), t).x;
-    if (!near_edge_c(t.x)) return make_float2(0.f, 0.f);
+    float2 xc;
+    directivity2_fast(tab, make_float2(ct, ct), xc);
+    if (!near_edge(xc.x)) return make_float2(0.f, 0.f);
     const float thc = theta2_centred(make_float2(ct, ct)).x;
+    const int i_fast = fast_bin(thc);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
+    if (i_exact == i_fast) return make_float2(0.f, 0.f);
     const float r = r2 * rinv;
     const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
     const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
-    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - d_fast);
+    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - dir_in_bin(tab, thc, i_fast));
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 
@@ -187,7 +185,10 @@ struct PairGeom {
 // The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
 // records whether any of the thread's points has its theta next to a bin edge; that rare case
 // recomputes the pairs' geometry to find which points, and corrects them one by one.  RED:
-// reduce the phase before sin/cos (see kUnreducedPhaseMax).
+// reduce the phase before sin/cos (see kUnreducedPhaseMax).  This body keeps the theta-binned
+// directivity (acos polynomial and MUFU square root): with three coordinates per point it has
+// no registers left for the cos(theta)-indexed table's two dependent lookups, which spill here
+// and made the batched kernel 12 % slower, while the rows body (field_rows.cuh) gains 8 %.
 template <int ST, int SUM, int PAIRS, bool UD, bool RED>
 __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, float3 n0,
                                                   float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
@@ -201,7 +202,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         if constexpr (UD) ns = sm.ns[j];
         else v2 = sm.v2[j];
     }
-    float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
+    bool any_near = false;
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
@@ -209,9 +210,9 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
-            float2 t;
-            w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
-            near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
+            float2 xc;
+            w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
+            any_near |= near_edge(xc.x) | near_edge(xc.y);
         }
         const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -228,12 +229,11 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         }
     }
     if constexpr (ST == SRC_T4010A1) {
-        if (near_min < kCTabMargin) {
+        if (any_near) {
 #pragma unroll
             for (int k = 0; k < 2 * PAIRS; ++k) {
                 const int q = k >> 1, h = k & 1;
-                const float2 c = edge_correction<UD>(sm.dir, sm.cneg, sm.ccoef, v0, v1, v2, v3,
-                                                     v4, ns, n0,
+                const float2 c = edge_correction<UD>(sm.dir, v0, v1, v2, v3, v4, ns, n0,
                                                      lane_of(NP[q], h), lane_of(PX[q], h),
                                                      lane_of(PY[q], h), lane_of(PZ[q], h));
                 if constexpr (SUM == SUM_PLAIN) {

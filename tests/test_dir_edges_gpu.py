@@ -1,9 +1,10 @@
 """Pairs next to a directivity bin edge (10-degree multiples from 20 to 90 degrees), where the
-kernels' cos(theta)-indexed directivity switches sides and the exact edge path takes over, in
-both field bodies: the general one (scatter points, one source per point, so each pair's value
-is checked on its own) and the rows tiling (a large grid with sources placed on rays through
-one grid node at the edge angles).  Offsets from the edge run from 0 to 1e-4 rad on both sides,
-through the 4e-6 margin in cos(theta) of the exact path."""
+fast directivity switches bins and the exact edge path takes over, in both field bodies: the
+general one (scatter points, theta-binned directivity; one source per point, so each pair's
+value is checked on its own) and the rows tiling (cos(theta)-indexed table; a large grid with
+sources placed on rays through one grid node at the edge angles).  Offsets from the edge run
+from 0 to 1e-4 rad on both sides, through the edge paths' margins (1e-5 rad in theta, 4e-6 in
+cos(theta))."""
 import numpy as np
 import pytest
 
