@@ -1,13 +1,14 @@
 // Many independent field jobs of uneven size in one persistent launch, replayed from a CUDA
 // graph.  No reference counterpart: the reference evaluates one AFC_Calculate at a time
 // (calculator/cpu_calculator.rs:43-56); every job here computes exactly that field with the
-// same per-block body as the single-job kernel (field_body.cuh).
+// same per-block bodies as the single-job kernels (field_body.cuh, field_rows.cuh).
 //
 // Plan (AFC_BatchCreate):
 //   * job table on the device: each job's source records, packed-arena offset, points (grid
 //     description or explicit points), field type and output pointer;
-//   * work items = (job, block of 2*PAIRS*256 points), sorted by cost (sources x points)
-//     descending so that the longest items start first and the short ones fill the tail;
+//   * work items = (job, block of 2*PAIRS*256 points, or one tile of the rows tiling for the
+//     grids the single-job launch tiles by rows), sorted by cost (sources x points) descending
+//     so that the longest items start first and the short ones fill the tail;
 //   * the autotuner (optional) runs the whole batch once per candidate point tile
 //     (PAIRS = 1, 2, 4 point pairs per thread) and keeps the fastest;
 //   * a CUDA graph is captured once: reset the work counter, pack every job's sources
@@ -27,6 +28,7 @@
 #include "afc_gpu.h"
 #include "afc_internal.h"
 #include "field_body.cuh"
+#include "field_rows.cuh"
 
 namespace afc {
 namespace batch {
@@ -51,7 +53,14 @@ struct JobDev {
 
 struct Item {
     int32_t job;
-    int32_t block;
+    int32_t block;  // flat block, or tile of the job's rows tiling
+};
+
+// How a job's points are split for the plan's point tile (rows_tiling).
+struct JobTile {
+    int32_t rows;  // 1: tiles of the rows tiling
+    int32_t tx_log2;
+    int64_t tiles0, tiles1;
 };
 
 __global__ void pack_all_kernel(int st, const JobDev* __restrict__ jobs,
@@ -63,7 +72,8 @@ __global__ void pack_all_kernel(int st, const JobDev* __restrict__ jobs,
 
 template <int ST, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
-    batch_kernel(const JobDev* __restrict__ jobs, const Item* __restrict__ items, int64_t n_items,
+    batch_kernel(const JobDev* __restrict__ jobs, const JobTile* __restrict__ tiles,
+                 const Item* __restrict__ items, int64_t n_items,
                  unsigned long long* __restrict__ counter, const PackedSource* __restrict__ arena) {
     __shared__ SmemTile sm;
     __shared__ long long s_item;
@@ -76,9 +86,15 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (it >= n_items) break;
         const Item w = items[it];
         const JobDev J = jobs[w.job];
-        const int64_t first = static_cast<int64_t>(w.block) * (kThreads * 2 * PAIRS);
-        block_points<ST, SUM_PLAIN, PAIRS>(sm, arena + J.src_off, J.n, J.is_grid != 0, J.g, J.pts,
-                                           J.m, first, J.field, J.out);
+        const JobTile T = tiles[w.job];
+        if (T.rows) {
+            block_rows<ST, SUM_PLAIN, PAIRS>(sm, arena + J.src_off, J.n, J.g, T.tx_log2, T.tiles0,
+                                             T.tiles1, w.block, J.field, J.out);
+        } else {
+            const int64_t first = static_cast<int64_t>(w.block) * (kThreads * 2 * PAIRS);
+            block_points<ST, SUM_PLAIN, PAIRS>(sm, arena + J.src_off, J.n, J.is_grid != 0, J.g,
+                                               J.pts, J.m, first, J.field, J.out);
+        }
     }
 }
 
@@ -92,6 +108,7 @@ struct Plan {
     double evals = 0;
     std::vector<JobDev> jobs;  // host copy
     JobDev* d_jobs = nullptr;
+    JobTile* d_tiles = nullptr;  // per job, for the current point tile
     Item* d_items = nullptr;
     int64_t n_items = 0;
     unsigned long long* d_counter = nullptr;
@@ -102,8 +119,8 @@ struct Plan {
 
 template <int ST, int PAIRS>
 cudaError_t launch_persistent(const Plan& p, int grid, cudaStream_t s) {
-    batch_kernel<ST, PAIRS><<<grid, kThreads, 0, s>>>(p.d_jobs, p.d_items, p.n_items, p.d_counter,
-                                                       p.d_arena);
+    batch_kernel<ST, PAIRS><<<grid, kThreads, 0, s>>>(p.d_jobs, p.d_tiles, p.d_items, p.n_items,
+                                                       p.d_counter, p.d_arena);
     return cudaGetLastError();
 }
 
@@ -135,18 +152,45 @@ cudaError_t launch_batch_kernel(const Plan& p, cudaStream_t s) {
     return launch_persistent<SRC_SPHERE, 4>(p, grid, s);
 }
 
-// Items for the current point tile (2*pairs*256 points per block), longest first.
+// Items for the current point tile (2*pairs*256 points per block, or rows tiles for the
+// grids the single-job launch tiles by rows), longest first.
 cudaError_t build_items(Plan& p) {
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * p.pairs;
     std::vector<std::pair<double, Item>> v;
+    std::vector<JobTile> tiles(static_cast<size_t>(p.n_jobs));
     for (int64_t j = 0; j < p.n_jobs; ++j) {
         const JobDev& J = p.jobs[j];
+        const double nsrc = static_cast<double>(J.n > 0 ? J.n : 1);
+        const RowsTiling t = J.is_grid ? rows_tiling(J.g, J.m, p.pairs) : RowsTiling{};
+        if (t.use) {
+            if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+            tiles[j] = JobTile{1, t.tx_log2, t.tiles0, t.tiles1};
+            const int64_t tx = 1LL << t.tx_log2;
+            for (int64_t b = 0; b < t.blocks; ++b) {
+                const int64_t t0 = b % t.tiles0, t1 = (b / t.tiles0) % t.tiles1;
+                const int64_t pts = std::min(tx, J.g.count[0] - t0 * tx) *
+                                    std::min(t.rows, J.g.count[1] - t1 * t.rows);
+                v.push_back({static_cast<double>(pts) * nsrc,
+                             Item{static_cast<int32_t>(j), static_cast<int32_t>(b)}});
+            }
+            continue;
+        }
+        tiles[j] = JobTile{0, 0, 0, 0};
         const int64_t blocks = (J.m + per_block - 1) / per_block;
         for (int64_t b = 0; b < blocks; ++b) {
             const int64_t pts = std::min(per_block, J.m - b * per_block);
-            v.push_back({static_cast<double>(pts) * static_cast<double>(J.n > 0 ? J.n : 1),
+            v.push_back({static_cast<double>(pts) * nsrc,
                          Item{static_cast<int32_t>(j), static_cast<int32_t>(b)}});
         }
+    }
+    if (p.n_jobs > 0) {
+        if (!p.d_tiles) {
+            const cudaError_t e = cudaMalloc(&p.d_tiles, sizeof(JobTile) * tiles.size());
+            if (e != cudaSuccess) return e;
+        }
+        const cudaError_t e = cudaMemcpy(p.d_tiles, tiles.data(), sizeof(JobTile) * tiles.size(),
+                                         cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
     }
     std::stable_sort(v.begin(), v.end(),
                      [](const std::pair<double, Item>& a, const std::pair<double, Item>& b) {
@@ -194,6 +238,7 @@ void destroy(Plan* p) {
     if (p->cap) cudaStreamSynchronize(p->cap);
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->d_jobs) cudaFree(p->d_jobs);
+    if (p->d_tiles) cudaFree(p->d_tiles);
     if (p->d_items) cudaFree(p->d_items);
     if (p->d_counter) cudaFree(p->d_counter);
     if (p->d_arena) cudaFree(p->d_arena);
