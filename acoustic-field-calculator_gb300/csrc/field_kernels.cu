@@ -19,7 +19,9 @@
 //     are corrected after the source, off the interleaved path.
 //   * On grids with more than one point along the second axis a thread's points are
 //     consecutive along that axis (field_rows_kernel), so the offsets along the other two axes
-//     are computed once per source and thread.
+//     are computed once per source and thread.  That body takes the directivity from a
+//     cos(theta)-indexed table (no acos, no MUFU square root; propagate.cuh); the general body
+//     keeps the theta-binned one, whose temporaries its registers can hold.
 //   * When every source of a tile points the same way as source 0 (a planar array), cos(theta)
 //     comes from n.x - n.s with n.x precomputed per point and n.s per source: two FP32
 //     operations per pair instead of four.  Each block decides this per tile.

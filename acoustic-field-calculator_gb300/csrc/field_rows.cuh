@@ -7,9 +7,11 @@
 // grid's axis order; per source and thread, the offsets along the first and third axes, the
 // sum of their squares and (for tiles of unequal directions) their part of n.d are computed
 // once, and each point pair only adds the offset along the second axis: three fewer packed
-// FP32 instructions per pair than the general body (field_body.cuh), whose math this is.
-// Points and the order of the sum over sources are the reference's
-// (observe_area/grid/grid_area.rs:59-229, system/uniform_medium.rs:111-128).
+// FP32 instructions per pair than the general body (field_body.cuh), whose math this is.  The
+// directivity comes from the cos(theta)-indexed table (directivity2_ctab), and a thread keeps
+// the smallest |c - L| of its points for the exact edge path.  Points and the order of the sum
+// over sources are the reference's (observe_area/grid/grid_area.rs:59-229,
+// system/uniform_medium.rs:111-128).
 #pragma once
 
 #include <cuda_runtime.h>
