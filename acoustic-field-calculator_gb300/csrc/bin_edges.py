@@ -3,20 +3,37 @@
 
 The T4010A1 directivity (acoustic-field-calculator/src/core/wave_sources/t4010a1.rs:107-120)
 takes its bin from the f32 theta as i = ceil(theta / ANGLE_DIV) (0 -> 1.0, > 9 -> 0.0), with
-theta = acos(c) rounded to f32 and ANGLE_DIV = f32(pi) / 18 in f32.  theta is monotone
-non-increasing in c, and f32 division and ceil are monotone, so the bin is a step function of
-the float c: for b = 1..10 there is a largest float L_b with bin(L_b) >= b, and for every
-float c
+theta = f32::acos(c) and ANGLE_DIV = f32(pi) / 18 in f32.  Rust's f32::acos is the platform
+libm's acosf (glibc on Linux), which is not correctly rounded: near a bin edge its last-ulp
+rounding decides the bin, and a pair there contributes a whole directivity jump (up to 17 % of
+its term).  The thresholds therefore follow glibc's acosf itself, called here through ctypes.
+theta is monotone non-increasing in c, and f32 division and ceil are monotone, so the bin is a
+step function of the float c: for b = 1..10 there is a largest float L_b with bin(L_b) >= b,
+and for every float c
 
     bin(c) (clipped to 0..10) = #{b : c <= L_b}        (a NaN c compares false: bin 0)
 
-This script finds L_b by bisection over the ordered float32 values of [-1, 1], with theta
-taken as float64 arccos rounded to float32 (the correctly rounded acosf), then checks the
-identity exhaustively on 2^17 floats around every threshold.  Run: python bin_edges.py
+This script finds L_b by bisection over the ordered float32 values of [-1, 1], then checks the
+identity exhaustively on 2^17 floats around every threshold (which also checks that acosf is
+monotone there).  Run: python bin_edges.py
 """
+import ctypes
+import ctypes.util
 import numpy as np
 
 ANGLE_DIV = np.float32(np.float32(np.pi) / np.float32(18.0))
+
+_LIBM = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+_LIBM.acosf.argtypes = [ctypes.c_float]
+_LIBM.acosf.restype = ctypes.c_float
+
+
+def acosf_libm(c):
+    """The platform libm's acosf, elementwise (float32 in, float32 out)."""
+    c = np.asarray(c, dtype=np.float32)
+    f = _LIBM.acosf
+    return np.fromiter((f(v) for v in c.ravel().tolist()), dtype=np.float32,
+                       count=c.size).reshape(c.shape)
 
 
 def _key_to_f32(key):
@@ -35,7 +52,7 @@ def ref_bin(c):
     """The reference's bin for float32 cos(theta) values, clipped to 0..10 (NaN -> 0)."""
     c = np.asarray(c, dtype=np.float32)
     with np.errstate(invalid="ignore"):
-        theta = np.arccos(c.astype(np.float64)).astype(np.float32)
+        theta = acosf_libm(c)
         q = np.ceil(theta / ANGLE_DIV)  # float32 division, round to nearest
     q = np.where(np.isnan(q), 0.0, q)
     return np.clip(q, 0, 10).astype(np.int64)
@@ -70,7 +87,7 @@ def check(ths, window=1 << 16):
         c = _key_to_f32(keys)
         assert np.array_equal(ref_bin(c), bin_from_thresholds(c, ths)), t
     rng = np.random.default_rng(0)
-    c = rng.uniform(-1.0, 1.0, 1 << 22).astype(np.float32)
+    c = rng.uniform(-1.0, 1.0, 1 << 20).astype(np.float32)
     assert np.array_equal(ref_bin(c), bin_from_thresholds(c, ths))
     return True
 

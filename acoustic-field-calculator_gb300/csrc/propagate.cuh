@@ -6,19 +6,22 @@
 //     w = A_j D exp(-alpha_j r) / r,   phase = phi_j + k_j r
 // and the contribution w * (cos phase, sin phase).
 //
-// Fast path (every pair): rsqrt / ex2 / sqrt / sin / cos on the MUFU pipe (PTX .approx.ftz),
-// theta from an own-fit polynomial, everything else in FP32, two points at a time with the
-// sm_100 packed f32x2 instructions where both points take the same operation.
+// Fast path (every pair): rsqrt / ex2 / sin / cos on the MUFU pipe (PTX .approx.ftz), the
+// directivity from theta (an own-fit acos polynomial times a MUFU sqrt; the general body) or
+// straight from cos(theta) (a cubic table; the rows body), everything else in FP32, two points
+// at a time with the sm_100 packed f32x2 instructions where both points take the same
+// operation.
 //
-// The T4010A1 directivity is piecewise in 10-degree bins and jumps at 30, 40, 60 and 90
-// degrees (by 0.016, 0.003, 0.047 and 0.164).  A theta within rounding of a bin edge can land
-// in a different bin than the reference's f32 arithmetic puts it, which changes that pair's
-// term by up to 16 %.  Pairs whose fast theta lies within kEdgeMargin of an edge therefore take
-// the exact bin: cos(theta) by the reference's f32 operations (no FMA, IEEE sqrt and division),
-// then compared with the ten float thresholds kBinCos1..10 at which the reference's bin
-// ceil(acos(c) / ANGLE_DIV) -- acos correctly rounded to f32 -- steps (derived and checked
-// exhaustively around every edge in bin_edges.py).  The cubic of that bin is evaluated at the
-// fast theta (within 3e-6 rad).  No double-precision operation is involved.
+// The T4010A1 directivity is piecewise in 10-degree bins and jumps at its edges (by up to
+// 0.17).  A pair within rounding of a bin edge can land in a different bin than the
+// reference's f32 arithmetic puts it, which changes that pair's term by up to 17 %.  Pairs
+// next to an edge therefore take the exact bin: cos(theta) by the reference's f32 operations
+// (no FMA, IEEE sqrt and division), then compared with the ten float thresholds kBinCos1..10
+// at which the reference's bin ceil(acosf(c) / ANGLE_DIV) steps -- with acosf the one the
+// reference calls, glibc's (Rust's f32::acos), whose last-ulp rounding near an edge decides
+// the bin (derived and checked exhaustively around every edge in bin_edges.py).  The cubic of
+// that bin is evaluated at the fast theta (within 3e-6 rad).  No double-precision operation
+// is involved.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -61,10 +64,10 @@ constexpr float kBinCos3 = 0x1.e11f62p-1f;    // 0.939692557
 constexpr float kBinCos4 = 0x1.bb67acp-1f;    // 0.866025329
 constexpr float kBinCos5 = 0x1.8836f8p-1f;    // 0.766044378
 constexpr float kBinCos6 = 0x1.491b72p-1f;    // 0.642787516
-constexpr float kBinCos7 = 0x1.fffffap-2f;    // 0.499999911
+constexpr float kBinCos7 = 0x1.fffff8p-2f;    // 0.499999881
 constexpr float kBinCos8 = 0x1.5e3a82p-2f;    // 0.342020065
-constexpr float kBinCos9 = 0x1.63a194p-3f;    // 0.17364803
-constexpr float kBinCos10 = -0x1.ddde98p-23f;  // -2.2252533e-07
+constexpr float kBinCos9 = 0x1.63a196p-3f;    // 0.173648044
+constexpr float kBinCos10 = -0x1.ddde9cp-23f;  // -2.2252536e-07
 
 // acos(c) = sqrt(1 - c) * Q(c); Q of degree 5 fitted in fit_acos.py (float32 error <= 1.7e-6
 // rad on [-0.03, 1]; for c in [-1, -0.02] it stays between 1.59 and 2.75 rad, i.e. beyond 90
@@ -85,9 +88,9 @@ constexpr float kAcos5 = -0.0045999325811862946f;
 // of 0.
 #define AFC_DIR_TABLE_INIT \
     { \
-        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
-        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
-        {0x1.0p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.p+0f, 0.f, 0.f, 0.f},  \
+        {0x1.p+0f, 0.f, 0.f, 0.f},  \
         {0x1.ea25b8p-1f, -0x1.6dfba4p-1f, -0x1.4b12a6p+1f, 0x1.e10248p-11f},  \
         {0x1.9c91eep-1f, -0x1.113aaap+0f, -0x1.027ceep+0f, 0x1.6570fep-13f},  \
         {0x1.33e156p-1f, -0x1.37c58cp+0f, 0x1.b362dep-2f, 0x1.172b94p+2f},  \
@@ -116,7 +119,7 @@ constexpr float kAcos5 = -0.0045999325811862946f;
         {0.f, 0.f, 0.f, 0.f},  \
         {0.f, 0.f, 0.f, 0.f},  \
         {0.f, 0.f, 0.f, 0.f},  \
-        {0x1.0p+0f, 0.f, 0.f, 0.f} \
+        {0x1.p+0f, 0.f, 0.f, 0.f} \
     }
 // The fast path indexes the table with the low five bits of the rounded bin float (theta < 2.8
 // rad, so the bin is at most 16, or wraps to 31 just below 0).

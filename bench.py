@@ -13,7 +13,9 @@ Arms
              uploads the sources and downloads the 134 MB complex field into the field
              buffer (pinned host memory) -- wall-clock per call, the call synchronises.
              `cpu_baseline`: the oracle (C restatement of the reference CPU calculator,
-             OpenMP over points) on a bounded z-slab of the same grid, on this host's cores.
+             OpenMP over points) on a bounded z-slab of the same grid, on this host's cores;
+             its `parity` checks the timed launches' field on that slab against the oracle's
+             (max |p - p_ref| over the slab's peak |p_ref|, bar 1e-4).
   reference  the reference's CPU calculator restated in C (the oracle: the Rust reference
              cannot be built here), all host threads, each step one bounded z-slab sample.
 
@@ -104,31 +106,42 @@ def cpu_slab(w, n_planes: int):
 
 
 def cpu_rate(w, pts, repeats=1):
+    """Time the oracle's f32 field on pts; returns (times, threads, the last field)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O  # the CPU baseline only
 
     O.field_f32(1, w.sources, w.k, w.atten, pts[:256], O.FIELD_COMPLEX)  # warm
     times = []
+    field = None
     for _ in range(repeats):
         t0 = time.perf_counter()
-        O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_COMPLEX)
+        field = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_COMPLEX)
         times.append(time.perf_counter() - t0)
-    return times, O.max_threads()
+    return times, O.max_threads(), field
 
 
-def cpu_baseline(w, target_s=12.0):
+def cpu_baseline(w, gpu_field=None, target_s=12.0):
+    """The oracle timed on a z-slab of the grid.  gpu_field (the timed launches' output, host
+    complex64, grid order) is checked against the oracle's slab as it goes: the bar is 1e-4 of
+    the slab's peak |p|."""
     # calibrate on a quarter plane, then size the slab to ~target_s of CPU work
     probe = cpu_slab(w, 1)[:16384]
-    t, threads = cpu_rate(w, probe)
+    t, threads, _ = cpu_rate(w, probe)
     per_pt = t[0] / len(probe)
     planes = int(max(1, min(64, target_s / (per_pt * 65536))))
     pts = cpu_slab(w, planes)
-    t, threads = cpu_rate(w, pts)
+    t, threads, ref = cpu_rate(w, pts)
     evals = len(pts) * w.n
-    return {"value": evals / t[0], "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{planes} z-plane(s) of the 256^3 grid = {len(pts)} points x {w.n} "
-                      f"sources ({evals:.3e} evals) in {t[0]:.2f} s, oracle f32, "
-                      f"{threads} OpenMP threads"}
+    out = {"value": evals / t[0], "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{planes} z-plane(s) of the 256^3 grid = {len(pts)} points x {w.n} "
+                     f"sources ({evals:.3e} evals) in {t[0]:.2f} s, oracle f32, "
+                     f"{threads} OpenMP threads"}
+    if gpu_field is not None and len(gpu_field) >= len(ref):
+        err = float(np.max(np.abs(gpu_field[:len(ref)] - ref)) / np.max(np.abs(ref)))
+        out["parity"] = {"max_abs_err_over_peak": err, "bar": 1e-4, "pass": err <= 1e-4,
+                         "points": len(ref), "against": "oracle f32 (the reference CPU "
+                                                       "calculator's restatement)"}
+    return out
 
 
 def run_reference(args):
@@ -377,7 +390,10 @@ def run_ours(args):
             "gpu_launches": int(launches), "roofline": roofline, "clocks": clock_summary,
             "wall_s_timed": wall}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w)
+        # the timed launches' field on the first 64 planes (at most the slab the CPU runs)
+        slab = min(m, 64 * count * count)
+        gpu_field = out[:2 * slab].cpu().numpy().view(np.complex64)
+        line["cpu_baseline"] = cpu_baseline(w, gpu_field if count == 256 else None)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

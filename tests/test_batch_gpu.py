@@ -13,12 +13,6 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-@pytest.fixture(autouse=True)
-def _correctly_rounded_acos():
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        yield
-
-
 def _small_jobs():
     jobs = W.batch_jobs(seed=21, n_jobs=10, m_range=(1.0, 4e4), counts=(249, 498))
     # add edge cases: one point, one source, no sources

@@ -1,6 +1,8 @@
 """The exact directivity-bin thresholds of the field kernels (kBinCos1..10 in propagate.cuh)
-reproduce the reference's bin ceil(acos(c) / ANGLE_DIV) for every float c around each edge,
-with acos correctly rounded to f32 (the oracle's correctly rounded mode)."""
+reproduce the reference's bin ceil(acosf(c) / ANGLE_DIV) for every float c around each edge,
+with acosf the platform libm's (glibc's, which Rust's f32::acos calls; the oracle's default
+mode).  Run on the GPU machine too, this also checks that its libm agrees with the one the
+thresholds were derived with."""
 import os
 import re
 import sys
@@ -38,6 +40,5 @@ def test_thresholds_reproduce_the_oracle_bins_around_every_edge():
     rng = np.random.default_rng(1)
     c = np.concatenate([c, rng.uniform(-1, 1, 200000).astype(np.float32),
                         np.float32([1.0, -1.0, 0.0, -0.0, np.nan])])
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        ref = O.bins_of_cos(c)
+    ref = O.bins_of_cos(c)
     assert np.array_equal(BE.bin_from_thresholds(c, ths), ref)

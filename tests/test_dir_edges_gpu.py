@@ -17,12 +17,6 @@ EDGES_DEG = np.arange(20, 91, 10)
 OFFSETS = np.array([-1e-4, -1e-5, -3e-6, -1e-6, -2e-7, 0.0, 2e-7, 1e-6, 3e-6, 1e-5, 1e-4])
 
 
-@pytest.fixture(autouse=True)
-def _correctly_rounded_acos():
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        yield
-
-
 def _directions(rng, tilted, n):
     if not tilted:
         return np.tile(np.array([0.0, 0.0, 1.0]), (n, 1))

@@ -18,16 +18,6 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-@pytest.fixture(autouse=True)
-def _correctly_rounded_acos():
-    """The oracle's acos is rounded correctly here, as the GPU's near-bin-edge path rounds it:
-    with the platform's glibc acosf the directivity bin of a pair whose theta lies within one
-    ulp of a bin edge follows that libm's rounding (test_oracle_known_answers.py covers how
-    rarely the two differ)."""
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        yield
-
-
 def rel_err(p, ref):
     p = np.asarray(p)
     ref = np.asarray(ref)

@@ -46,8 +46,7 @@ def test_nls_matches_dense_f64(gpu, kind, n, m):
     t_gpu = time.perf_counter() - t0
     got = s.records().copy()
     t0 = time.perf_counter()
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        ref = O.nls_f64(kind, 1, rec, k, a, foci, amps).reshape(-1, 9)
+    ref = O.nls_f64(kind, 1, rec, k, a, foci, amps).reshape(-1, 9)
     t_ref = time.perf_counter() - t0
     np.testing.assert_array_equal(got[:, 6], rec[:, 6])
     p_gpu = np.abs(O.field_f64(1, got, k, a, foci))

@@ -11,12 +11,6 @@ import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True)
-def _correctly_rounded_acos():
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        yield
-
-
 def _geometries():
     g1 = W.tiled_array(1, 1)
     g4 = W.tiled_array(2, 2)

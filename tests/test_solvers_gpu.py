@@ -115,8 +115,7 @@ def test_greedy_matches_oracle(gpu, m, div):
     s = _system(afc, w)
     afc.Optimizer.greedy(s, foci, amps, div)
     got = s.records().copy()
-    with O.acos_mode(O.ACOS_CORRECTLY_ROUNDED):
-        ref = O.greedy_f32(1, w.sources, w.k, w.atten, foci, amps, div).reshape(-1, 9)
+    ref = O.greedy_f32(1, w.sources, w.k, w.atten, foci, amps, div).reshape(-1, 9)
     np.testing.assert_array_equal(got[:, 6], w.sources[:, 6])
     cands = np.unique(ref[:, 7])
     assert np.all(np.isin(got[:, 7], cands)) or div > len(cands)
