@@ -17,7 +17,10 @@ side, the smaller bin) and 2 i + 1 for c <= L, and the kernels take the side fro
 c - L (negedge[i] = -L; intervals without an edge store L = -1e30, so only entry 2 i is used).
 Pairs whose fast c lies within kCTabMargin of L are recomputed exactly by the kernels' edge
 path.  Intervals below -1/K give 0 (bin 10); entries from c = 1 on (a unit cosine rounded up,
-or a non-unit direction, where the reference's acos is NaN and its bin 0) give 1.
+or a non-unit direction, where the reference's acos is NaN and its bin 0) give 1.  The two
+intervals around c = -1 carry the edge L = -1 (both sides 0): a point on a tilted source's back
+axis can have the reference's f32 c rounded below -1, where its acos is NaN and D is 1, so such
+pairs take the exact path too.
 
 Writes dir_ctable.inc beside this script and checks, over every interval and side, the float32
 Horner evaluation of the rounded coefficients against D_b(acos(c)) in float64.
@@ -76,6 +79,8 @@ def table():
         lo, hi = (i - BIAS) / K, (i - BIAS + 1) / K
         if hi <= 0 and lo < -1.0 / K:  # c < -1/K: theta beyond 90 degrees, bin 10
             bins[2 * i] = bins[2 * i + 1] = 10
+            if lo <= -1.0 < hi or hi == -1.0:  # the back axis: edge at c = -1
+                negedge[i] = np.float32(1.0)
             continue
         if lo >= 1.0:  # c >= 1: theta = 0 or the reference's acos is NaN, bin 0
             coef[2 * i] = coef[2 * i + 1] = (1.0, 0.0, 0.0, 0.0)

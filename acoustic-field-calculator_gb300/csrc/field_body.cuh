@@ -153,7 +153,7 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
     }
     float2 xc;
     directivity2_fast(tab, make_float2(ct, ct), xc);
-    if (!near_edge(xc.x)) return make_float2(0.f, 0.f);
+    if (!near_edge(xc.x) && !(ct < kBackAxisC)) return make_float2(0.f, 0.f);
     const float thc = theta2_centred(make_float2(ct, ct)).x;
     const int i_fast = fast_bin(thc);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
@@ -185,7 +185,9 @@ struct PairGeom {
 // The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
 // records whether any of the thread's points has its theta next to a bin edge; that rare case
 // recomputes the pairs' geometry to find which points, and corrects them one by one.  RED:
-// reduce the phase before sin/cos (see kUnreducedPhaseMax).  This body keeps the theta-binned
+// the careful variant, for tiles with a large phase bound or with some point possibly behind a
+// source: the phase is reduced before sin/cos (see kUnreducedPhaseMax), and a cos(theta) next
+// to -1 (kBackAxisC) also takes the exact path.  This body keeps the theta-binned
 // directivity (acos polynomial and MUFU square root): with three coordinates per point it has
 // no registers left for the cos(theta)-indexed table's two dependent lookups, which spill here
 // and made the batched kernel 12 % slower, while the rows body (field_rows.cuh) gains 8 %.
@@ -213,6 +215,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
             float2 xc;
             w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
             any_near |= near_edge(xc.x) | near_edge(xc.y);
+            if constexpr (RED) any_near |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
         }
         const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -333,7 +336,9 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
     for (int64_t t0 = s_lo; t0 < s_hi; t0 += kTile) {
         const int cnt = static_cast<int>((s_hi - t0) < kTile ? (s_hi - t0) : kTile);
         __syncthreads();
-        bool same_dir = true, small_phase = true;
+        // plain: every phase of the tile bounded for the unreduced path and every point in front
+        // of every source; otherwise the tile takes the careful variant (RED)
+        bool same_dir = true, plain = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
             const PackedSource s = src[t0 + j];
             // |phi' + k r| over the box: r is at most the distance to the farthest corner
@@ -341,7 +346,16 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
             const float fy = fmaxf(fabsf(sm.bbox[1] - s.a.y), fabsf(sm.bbox[4] - s.a.y));
             const float fz = fmaxf(fabsf(sm.bbox[2] - s.a.z), fabsf(sm.bbox[5] - s.a.z));
             const float rmax = sqrtf(fmaf(fz, fz, fmaf(fy, fy, fx * fx)));
-            small_phase = small_phase && fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y)) <= kUnreducedPhaseMax;
+            plain = plain && fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y)) <= kUnreducedPhaseMax;
+            if (ST == SRC_T4010A1) {
+                // the box's lowest n.(x - s) (per axis the corner n points away from): when it is
+                // not negative, every point is in front of the source, where cos(theta) >= 0
+                const float lx = s.b.x >= 0.f ? sm.bbox[0] : sm.bbox[3];
+                const float ly = s.b.y >= 0.f ? sm.bbox[1] : sm.bbox[4];
+                const float lz = s.b.z >= 0.f ? sm.bbox[2] : sm.bbox[5];
+                const float front = fmaf(s.b.z, lz - s.a.z, fmaf(s.b.y, ly - s.a.y, s.b.x * (lx - s.a.x)));
+                plain = plain && front >= 0.f;
+            }
             sm.v0[j] = make_float4(-s.a.x, -s.a.x, -s.a.y, -s.a.y);
             sm.v1[j] = make_float4(-s.a.z, -s.a.z, s.a.w, s.a.w);
             sm.v2[j] = make_float4(s.b.x, s.b.x, s.b.y, s.b.y);
@@ -352,9 +366,9 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
             same_dir = same_dir && s.b.x == n0.x && s.b.y == n0.y && s.b.z == n0.z;
         }
         const bool tile_same_dir = __syncthreads_and(same_dir);
-        const bool tile_small = __syncthreads_and(small_phase);
+        const bool tile_plain = __syncthreads_and(plain);
         if (ST == SRC_T4010A1 && tile_same_dir) {
-            if (tile_small) {
+            if (tile_plain) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
                     accumulate_source<ST, SUM, PAIRS, true, false>(sm, j, n0, PX, PY, PZ, NP, RE,
@@ -366,7 +380,7 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
                                                                   CRE, CIM);
             }
         } else {
-            if (tile_small) {
+            if (tile_plain) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
                     accumulate_source<ST, SUM, PAIRS, false, false>(sm, j, n0, PX, PY, PZ, NP, RE,

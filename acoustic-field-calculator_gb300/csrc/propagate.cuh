@@ -164,13 +164,16 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 
 // The reference's bin for one pair (uniform_medium.rs:113-116, t4010a1.rs:107-120): its f32
 // cos(theta) = ((nx dx + ny dy) + nz dz) / sqrt((dx dx + dy dy) + dz dz) without contraction,
-// IEEE sqrt and division, then the threshold count.
+// IEEE sqrt and division, then the threshold count (a NaN or out-of-range c gives bin 0, as
+// acosf's NaN does through Rust's `as usize`).
 static __device__ __noinline__ int exact_bin(float dx, float dy, float dz, float nx, float ny,
                                              float nz) {
     const float dist = __fsqrt_rn(
         __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
     const float dot = __fadd_rn(__fadd_rn(__fmul_rn(nx, dx), __fmul_rn(ny, dy)), __fmul_rn(nz, dz));
     const float c = __fdiv_rn(dot, dist);
+    // acosf of a c rounded below -1 (a point on a tilted source's back axis) is NaN: bin 0
+    if (c < -1.0f) return 0;
     return (c <= kBinCos1) + (c <= kBinCos2) + (c <= kBinCos3) + (c <= kBinCos4) +
            (c <= kBinCos5) + (c <= kBinCos6) + (c <= kBinCos7) + (c <= kBinCos8) +
            (c <= kBinCos9) + (c <= kBinCos10);
@@ -237,6 +240,12 @@ __device__ __forceinline__ float2 directivity2_fast(const float4* __restrict__ t
 
 __device__ __forceinline__ bool near_edge(float xc) { return fabsf(xc) > kEdgeBound; }
 
+// A fast cos(theta) below this can belong to a point on the source's back axis whose
+// reference cos(theta) rounds below -1, where acosf is NaN and the directivity 1 (bin 0); the
+// acos polynomial is not fitted there (theta beyond 92 degrees only needs D = 0), so such pairs
+// take the exact path.
+constexpr float kBackAxisC = -1.0f + 4.0e-6f;
+
 // ------------------------------------------------------------------ directivity from cos(theta)
 //
 // The hot loops take D as a function of c = cos(theta) directly, without theta = acos(c) and
@@ -284,7 +293,7 @@ __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, f
                                                float2 dy, float2 dz, float nx, float ny, float nz) {
     float2 xc;
     float2 d = directivity2_fast(tab, ct, xc);
-    const bool ex = near_edge(xc.x), ey = near_edge(xc.y);
+    const bool ex = near_edge(xc.x) || ct.x < kBackAxisC, ey = near_edge(xc.y) || ct.y < kBackAxisC;
     if (ex | ey) {
         const float2 thc = theta2_centred(ct);
         if (ex) d.x = directivity_exact(tab, thc.x, dx.x, dy.x, dz.x, nx, ny, nz);

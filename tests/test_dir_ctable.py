@@ -46,4 +46,8 @@ def test_edges_sit_in_the_interval_the_kernel_indexes():
         i = (int(np.floor(np.float64(e) * CT.K)) + CT.BIAS) & (CT.SIZE - 1)
         assert ne[i] == -e
         assert bins[2 * i] == b - 1 and bins[2 * i + 1] == b
-    assert np.count_nonzero(ne != np.float32(-CT.NO_EDGE)) == 8
+    # and the back axis: the two intervals that meet at c = -1
+    for c in (np.float32(-1.0), np.nextafter(np.float32(-1.0), np.float32(-2.0))):
+        i = (int(np.floor(np.float64(c) * CT.K)) + CT.BIAS) & (CT.SIZE - 1)
+        assert ne[i] == np.float32(1.0)
+    assert np.count_nonzero(ne != np.float32(-CT.NO_EDGE)) == 10

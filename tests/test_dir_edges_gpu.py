@@ -115,3 +115,64 @@ def test_rows_tiling_at_bin_edges(gpu, tilted):
     err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
     print(f"grid: rel {err:.2e}")
     assert err <= 1e-4
+
+
+def _ref_cos(d, n):
+    """The reference's f32 cos(theta): ((nx dx + ny dy) + nz dz) / sqrt((dx dx + dy dy) + dz dz)."""
+    f = np.float32
+    d = d.astype(f)
+    n = n.astype(f)
+    dist = np.sqrt(((d[:, 0] * d[:, 0]) + (d[:, 1] * d[:, 1])) + (d[:, 2] * d[:, 2]))
+    dot = ((n[:, 0] * d[:, 0]) + (n[:, 1] * d[:, 1])) + (n[:, 2] * d[:, 2])
+    return (dot / dist).astype(f)
+
+
+def _back_axis_sources(rng, nodes):
+    """One tilted source per node, 20-120 mm in front of it, so that the node sits exactly on
+    the source's back axis; returns records and the reference's f32 cos(theta) of each pair."""
+    m = len(nodes)
+    n = rng.normal(size=(m, 3)) * np.array([0.5, 0.5, 0.2]) + np.array([0, 0, 1.0])
+    n = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+    r = rng.uniform(20, 120, m).astype(np.float32)
+    pos = (nodes + r[:, None] * n.astype(np.float64)).astype(np.float32)
+    rec = W.t4010a1_records(pos, rng.uniform(0.5, 1.0, m).astype(np.float32),
+                            rng.uniform(-np.pi, np.pi, m).astype(np.float32))
+    rec[:, 3:6] = n
+    return rec, _ref_cos(nodes - pos, n)
+
+
+@pytest.mark.parametrize("body", ["general", "rows"])
+def test_back_axis_pairs(gpu, body):
+    """A point exactly on a tilted source's back axis: the reference's f32 cos(theta) rounds to
+    -1 or just below, and below -1 its acos is NaN, so the directivity is 1 (bin 0) instead of
+    0.  Both bodies route such pairs through the exact path."""
+    afc = gpu
+    rng = np.random.default_rng(31 if body == "general" else 32)
+    if body == "general":
+        nodes = np.stack([rng.uniform(-20, 20, 300), rng.uniform(-20, 20, 300),
+                          rng.uniform(100, 140, 300)], 1).astype(np.float32)
+        rec, c = _back_axis_sources(rng, nodes)
+        area = afc.ScatterArea()
+        area.add_observe_points(nodes)
+        pts = nodes
+    else:
+        counts, res = (96, 96, 72), 0.5
+        lo = np.array([-24.0, -24.0, 120.0], np.float32)
+        idx = np.stack([rng.integers(0, c_, 300) for c_ in counts], 1)
+        nodes = (lo + res * idx).astype(np.float32)
+        rec, c = _back_axis_sources(rng, nodes)
+        g = W.GridSpec(3, [(float(lo[j]), float(lo[j] + (counts[j] - 0.5) * res))
+                           for j in range(3)], res, (1, 2, 3))
+        area = afc.grid_from_spec(g)
+        glo, ghi = g.lo_hi()
+        pts = O.grid_points(3, glo, ghi, res, (1, 2, 3))
+    assert np.count_nonzero(c < -1) >= 20  # pairs whose reference directivity is 1
+    k = np.full(len(rec), W.wavenumber(), np.float32)
+    a = np.zeros(len(rec), np.float32)
+    s = afc.UniformSystem(300.0)
+    s.add_records(1, rec, k, a)
+    got = np.asarray(afc.GpuCalculator().calculate(s, area, afc.ComplexPressureFieldBuffer()))
+    ref = O.field_f32(1, rec, k, a, pts)
+    err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+    print(f"{body}: {np.count_nonzero(c < -1)} pairs with c < -1, rel {err:.2e}")
+    assert err <= 1e-4
