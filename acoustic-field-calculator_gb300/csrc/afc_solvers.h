@@ -68,4 +68,12 @@ int solve_nls(int kind, int st, float* src, const float* k, const float* atten, 
 int solve_apo(int st, float* src, const float* k, const float* atten, int64_t n,
               const float* foci, const float* amps, int64_t m, float lambda, std::string* err);
 
+// Matrix optimizers (multiple_foci/matrix/{horn,long}.rs) on the device, m <= kMatrixMaxFoci
+// (their m x m systems and Horn's m x 100 sequential SDP steps); write amplitudes and phases
+// into `src` in place.  Returns 0 on success, else fills *err.
+enum MatrixKind : int { MATRIX_HORN = 0, MATRIX_LONG = 1 };
+constexpr int64_t kMatrixMaxFoci = 256;
+int solve_matrix(int kind, int st, float* src, const float* k, const float* atten, int64_t n,
+                 const float* foci, const float* amps, int64_t m, std::string* err);
+
 }  // namespace afc

@@ -27,6 +27,7 @@
 
 #include "afc_internal.h"
 #include "afc_solvers.h"
+#include "dense_host.h"
 
 namespace afc {
 namespace {
@@ -220,33 +221,7 @@ cudaStream_t g_apo_stream = nullptr;
 int g_apo_device = -1;
 
 using cd = std::complex<double>;
-
-// Solve the Hermitian positive definite system a c = b (k x k, row-major, overwritten).
-bool hpd_solve(std::vector<cd>& a, std::vector<cd>& b, int k) {
-    for (int j = 0; j < k; ++j) {
-        double d = a[j * k + j].real();
-        for (int p = 0; p < j; ++p) d -= std::norm(a[j * k + p]);
-        if (!(d > 0.0)) return false;
-        d = std::sqrt(d);
-        a[j * k + j] = d;
-        for (int i = j + 1; i < k; ++i) {
-            cd s = a[i * k + j];
-            for (int p = 0; p < j; ++p) s -= a[i * k + p] * std::conj(a[j * k + p]);
-            a[i * k + j] = s / d;
-        }
-    }
-    for (int i = 0; i < k; ++i) {
-        cd s = b[i];
-        for (int p = 0; p < i; ++p) s -= a[i * k + p] * b[p];
-        b[i] = s / a[i * k + i].real();
-    }
-    for (int i = k - 1; i >= 0; --i) {
-        cd s = b[i];
-        for (int p = i + 1; p < k; ++p) s -= std::conj(a[p * k + i]) * b[p];
-        b[i] = s / a[i * k + i].real();
-    }
-    return true;
-}
+using dense::hpd_solve;
 
 }  // namespace
 

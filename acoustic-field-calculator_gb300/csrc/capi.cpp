@@ -464,6 +464,23 @@ void run_nls(int kind, void* handle, const void* foci, const float* amps, uint64
     if (rc != 0) set_error("%s", err.c_str());
 }
 
+void run_matrix(int kind, void* handle, const void* foci, const float* amps, uint64_t size,
+                int32_t st) {
+    if (!valid_source_type(st)) {
+        set_error("unknown source type %d", st);
+        return;
+    }
+    System* s = as_system(handle, st);
+    if (!s) return;
+    std::vector<float> f, a;
+    if (!unpack_foci(foci, amps, size, f, a)) return;
+    std::string err;
+    const int rc = solve_matrix(kind, st, s->src.data(), s->k.data(), s->atten.data(),
+                                static_cast<int64_t>(s->count()), f.data(), a.data(),
+                                static_cast<int64_t>(size), &err);
+    if (rc != 0) set_error("%s", err.c_str());
+}
+
 void unsupported(const char* name) {
     set_error("%s: this solver is not provided by the GB300 library (system left unchanged)",
               name);
@@ -872,8 +889,14 @@ void AFO_BesselBeam(void* handle, AfcVector3 point, AfcVector3 dir, float theta,
 void AFO_IFFT(void*, const char*, AfcVector3, AfcVector3, AfcVector3, float, float, int32_t) {
     unsupported("AFO_IFFT");
 }
-void AFO_Horn(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Horn"); }
-void AFO_Long(void*, const void*, const float*, uint64_t, int32_t) { unsupported("AFO_Long"); }
+void AFO_Horn(void* handle, const void* foci, const float* amps, uint64_t size,
+              int32_t source_type) {
+    run_matrix(MATRIX_HORN, handle, foci, amps, size, source_type);
+}
+void AFO_Long(void* handle, const void* foci, const float* amps, uint64_t size,
+              int32_t source_type) {
+    run_matrix(MATRIX_LONG, handle, foci, amps, size, source_type);
+}
 void AFO_APO(void* handle, const void* foci, const float* amps, uint64_t size, float lambda,
              int32_t source_type) {
     if (!valid_source_type(source_type)) {

@@ -146,28 +146,34 @@ void AFO_GS(void *handle, const void *foci, const float *amps, uint64_t size,
 void AFO_Naive(void *handle, const void *foci, const float *amps, uint64_t size,
                int32_t source_type);
 
-/* The remaining optimizer exports exist so that callers binding the whole reference ABI load
- * this library unchanged.  Their solvers are outside this library's scope: each call leaves
- * the system unchanged and records an "unsupported" error for AFC_GetLastError.
- *   capi/src/optimizer.rs:47-58 (BesselBeam), :60-77 (IFFT), :129-143 (Horn),
- *   :145-159 (Long), :161-177 (APO), :179-195 (GaussNewton), :197-213 (GradientDescent),
- *   :215-225 (LM), :227-243 (Greedy). */
+/* capi/src/optimizer.rs:47-58: Bessel beam phases (bessel.rs:30-51), host set-up */
 void AFO_BesselBeam(void *handle, AfcVector3 point, AfcVector3 dir, float theta,
                     int32_t source_type);
+/* capi/src/optimizer.rs:60-77: exported so that callers binding the whole reference ABI load
+ * this library unchanged.  Its solver (fft/ifft.rs, an image file and an FFT) is outside this
+ * library's scope: the call leaves the system unchanged and records an "unsupported" error for
+ * AFC_GetLastError. */
 void AFO_IFFT(void *handle, const char *path, AfcVector3 bottom_left, AfcVector3 top_left,
               AfcVector3 bottom_right, float spacing, float z, int32_t source_type);
+/* capi/src/optimizer.rs:129-143: Horn (matrix/horn.rs), on the GPU; at most 256 foci.  Its
+ * coordinate order comes from a fixed-seed generator (the reference's is unseeded). */
 void AFO_Horn(void *handle, const void *foci, const float *amps, uint64_t size,
               int32_t source_type);
+/* capi/src/optimizer.rs:145-159: Long (matrix/long.rs), on the GPU; at most 256 foci */
 void AFO_Long(void *handle, const void *foci, const float *amps, uint64_t size,
               int32_t source_type);
+/* capi/src/optimizer.rs:161-177: APO (nls/apo.rs), on the GPU */
 void AFO_APO(void *handle, const void *foci, const float *amps, uint64_t size, float lambda,
              int32_t source_type);
+/* capi/src/optimizer.rs:179-225: Gauss-Newton, gradient descent and Levenberg-Marquardt
+ * (nls/{gauss_newton,gradient_descent,lm}.rs), on the GPU */
 void AFO_GaussNewton(void *handle, const void *foci, const float *amps, uint64_t size,
                      int32_t source_type);
 void AFO_GradientDescent(void *handle, const void *foci, const float *amps, uint64_t size,
                          int32_t source_type);
 void AFO_LM(void *handle, const void *foci, const float *amps, uint64_t size,
             int32_t source_type);
+/* capi/src/optimizer.rs:227-243: greedy phase choice (combination/greedy.rs), on the GPU */
 void AFO_Greedy(void *handle, const void *foci, const float *amps, uint64_t size,
                 uint64_t phase_div, int32_t source_type);
 

@@ -305,3 +305,127 @@ def naive_f64(st, sources, k, atten, foci, amps):
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+# ------------------------------------------------------------------ matrix optimizers (float64)
+#
+# numpy restatements of acoustic-field-optimizer/src/multiple_foci/matrix/{horn,long}.rs in
+# float64, following the reference's steps literally (SVD pseudo-inverse, I - G G_pinv by
+# subtraction, QR solve of the normal equations).  Two things the reference leaves to chance or
+# to nalgebra's internals are fixed here as the GPU library fixes them:
+#   - Horn's coordinate order (an unseeded thread_rng in the reference): horn_indices;
+#   - the eigenpairs' order (ascending eigenvalue, as eigh returns them) and each eigenvector's
+#     unit factor: its first nonzero entry is real and positive (_phase_fixed).
+
+HORN_SEED = 0x243F6A8885A308D3
+_M64 = (1 << 64) - 1
+
+
+def horn_indices(m: int, steps: int, seed: int = HORN_SEED) -> np.ndarray:
+    """Coordinate t = floor(m v_t) in float32, v_t = (x_t >> 9) 2^-23 (rand 0.8's f32 draw in
+    [0, 1)), x_t the high 32 bits of the t-th SplitMix64 output from `seed`."""
+    out = np.empty(steps, dtype=np.int64)
+    state = seed
+    for t in range(steps):
+        state = (state + 0x9E3779B97F4A7C15) & _M64
+        z = state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        z ^= z >> 31
+        v = np.float32((z >> 32) >> 9) * np.float32(1.0 / 8388608.0)
+        out[t] = min(int(np.float32(m) * v), m - 1)
+    return out
+
+
+def _phase_fixed(v: np.ndarray) -> np.ndarray:
+    """Columns scaled so that each one's first nonzero entry is real and positive (eigh's
+    ascending eigenvalue order is the other half of the convention)."""
+    v = v.copy()
+    for j in range(v.shape[1]):
+        nz = np.flatnonzero(v[:, j])
+        if len(nz) == 0:
+            continue
+        a = v[nz[0], j]
+        v[:, j] *= np.conj(a) / abs(a)
+        v[nz[0], j] = abs(a)
+    return v
+
+
+def _matrix_setup(st, sources, k, atten, foci, amps):
+    stride = 9 if st == SRC_T4010A1 else 6
+    s = np.array(sources, dtype=np.float32, copy=True).reshape(-1, stride)
+    s[:, 7 if st == SRC_T4010A1 else 4] = 0.0  # horn.rs:74-76, long.rs:51-53
+    foci = np.ascontiguousarray(foci, dtype=np.float32).reshape(-1, 3)
+    amps = np.ascontiguousarray(amps, dtype=np.float32).astype(np.float64)
+    g = build_g_f64(st, s, k, atten, foci)
+    return s, g, amps, stride
+
+
+def _write_drive(st, s, q):
+    """horn.rs:122-128, long.rs:99-104: amp *= |q_j| / camax(q) (largest |re| + |im|),
+    phase = arg q_j."""
+    iamp, iphase = (6, 7) if st == SRC_T4010A1 else (3, 4)
+    max_coeff = np.max(np.abs(q.real) + np.abs(q.imag))
+    s[:, iamp] = (s[:, iamp].astype(np.float64) * np.abs(q) / max_coeff).astype(np.float32)
+    s[:, iphase] = np.angle(q).astype(np.float32)
+    return s
+
+
+def horn_mm_f64(g, amps, alpha=1e-5):
+    """MM = P (I - G G_pinv) P with G_pinv = V diag(s / (s^2 + alpha^2)) U^H (horn.rs:60-69,
+    83-84), and G_pinv itself."""
+    u, sv, vh = np.linalg.svd(g, full_matrices=False)
+    g_pinv = vh.conj().T @ np.diag(sv / (sv * sv + alpha * alpha)) @ u.conj().T
+    p = np.diag(amps).astype(np.complex128)
+    mm = p @ (np.eye(len(amps)) - g @ g_pinv) @ p
+    return mm, g_pinv
+
+
+def horn_sdp_f64(mm, idx, lam=0.8):
+    """horn.rs:84-117: X = I, then one coordinate ii per step."""
+    m = mm.shape[0]
+    x = np.eye(m, dtype=np.complex128)
+    for ii in idx:
+        rest = np.r_[0:ii, ii + 1:m]
+        xb = x[np.ix_(rest, rest)] @ mm[rest, ii]
+        gamma = np.vdot(xb, mm[rest, ii])
+        if gamma.real > 0:
+            xb = xb * -np.sqrt(lam / gamma.real)
+            x[ii, rest] = xb.conj()
+            x[rest, ii] = xb
+        else:
+            x[ii, rest] = 0.0
+            x[rest, ii] = 0.0
+    return x
+
+
+def horn_f64(st, sources, k, atten, foci, amps, repeat=100):
+    """Horn (matrix/horn.rs:71-129) in float64; returns (updated sources, complex q)."""
+    s, g, amps, stride = _matrix_setup(st, sources, k, atten, foci, amps)
+    m = len(amps)
+    mm, g_pinv = horn_mm_f64(g, amps)
+    x = horn_sdp_f64(mm, horn_indices(m, m * repeat))
+    w, v = np.linalg.eigh(x)
+    u = _phase_fixed(v)[:, int(np.argmax(w))]
+    q = g_pinv @ (amps * u)
+    return _write_drive(st, s, q).reshape(-1), q
+
+
+def long_f64(st, sources, k, atten, foci, amps):
+    """Long (matrix/long.rs:48-105) in float64; returns (updated sources, complex q).
+    symmetric_eigen reads R's lower triangle and real diagonal, as eigh (UPLO='L') does."""
+    s, g, amps, stride = _matrix_setup(st, sources, k, atten, foci, amps)
+    m, n = g.shape
+    denomi = g.sum(axis=1)
+    x = (amps[:, None] * g.conj() / denomi[:, None]).T
+    r = g @ x
+    w, v = np.linalg.eigh(r, UPLO="L")
+    e_arg = np.angle(_phase_fixed(v)[int(np.argmax(w)), :])
+    sigma = np.sqrt((np.abs(g) * amps[:, None]).sum(axis=0) / m)
+    gg = np.vstack([g, np.diag(sigma).astype(np.complex128)])
+    f = np.concatenate([amps * np.exp(1j * e_arg), np.zeros(n)])
+    gtg = gg.conj().T @ gg
+    gtf = gg.conj().T @ f
+    qq, rr = np.linalg.qr(gtg)
+    q = np.linalg.solve(rr, qq.conj().T @ gtf)
+    return _write_drive(st, s, q).reshape(-1), q

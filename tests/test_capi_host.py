@@ -182,7 +182,9 @@ def test_unsupported_optimizers_leave_system_unchanged(afc_mod):
     s.add_records(1, W.t4010a1_records(W.unit_array()[:5], 1.0, 0.25))
     before = s.records().copy()
     with pytest.raises(RuntimeError, match="not provided"):
-        afc_mod.Optimizer.horn(s, [(0, 0, 100)], [1.0])
+        v = afc_mod.Vector3
+        afc_mod.Optimizer.ifft(s, "pattern.bmp", v((0, 0, 0)), v((0, 10, 0)), v((10, 0, 0)), 1.0,
+                               100.0)
     np.testing.assert_array_equal(s.records(), before)
 
 
