@@ -8,6 +8,7 @@
 // -ffp-contract=off.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -130,10 +131,16 @@ struct System {
     size_t count() const { return k.size(); }
 };
 
+// Scatter-area versions come from one process-wide counter, so that a (handle, version) pair
+// never repeats: an area freed and another created at the same address get different
+// versions, and a calculator's cached device copy of the old points is not reused.
+std::atomic<uint64_t> g_scatter_version{0};
+uint64_t next_scatter_version() { return g_scatter_version.fetch_add(1) + 1; }
+
 struct Scatter {
     uint32_t magic = MAGIC_SCATTER;
     std::vector<float> pts;
-    uint64_t version = 0;  // bumped on every added point
+    uint64_t version = next_scatter_version();  // renewed on every added point
 };
 
 struct Grid {
@@ -727,7 +734,7 @@ void AFC_ScatterAddObservePoint(void* handle, AfcVector3 p) {
     s->pts.push_back(p.x);
     s->pts.push_back(p.y);
     s->pts.push_back(p.z);
-    ++s->version;
+    s->version = next_scatter_version();
 }
 
 void AFC_FreeScatterArea(void* handle) {

@@ -216,6 +216,26 @@ def test_scatter_points_added_between_calls(gpu):
     assert rel_err(first, ref[:100]) <= TOL
 
 
+def test_new_scatter_area_after_free_is_not_the_cached_one(gpu):
+    """An area freed and a new one created (often at the same address) with as many points: the
+    calculator must upload the new points, not reuse its device copy of the old ones."""
+    import gc
+
+    afc = gpu
+    rng = np.random.default_rng(13)
+    rec, k, a = random_sources(rng, 0, 20)
+    s = make_system(afc, 0, rec, k, a)
+    calc = afc.CpuCalculator()
+    f = afc.PressureFieldBuffer()
+    for _ in range(4):
+        pts = random_points(rng, 100)
+        area = scatter(afc, pts)
+        out = calc.calculate(s, area, f).copy()
+        assert rel_err(out, np.abs(O.field_f32(0, rec, k, a, pts))) <= TOL
+        del area
+        gc.collect()
+
+
 def test_focal_point_then_field(gpu):
     """Reference example flow: AFO_FocalPoint, then the pressure on an XY slice."""
     afc = gpu
