@@ -12,8 +12,9 @@
 //   the reference forms I - G G_pinv by subtraction; its entries (about a^2 / |K|, 1e-9) lie
 //   far below f32 resolution, so its MM is rounding noise.  The form here keeps MM to double
 //   accuracy.  The SDP's coordinate updates (horn.rs:87-117) are invariant to the scale of MM;
-//   they run as one device block in double, m * 100 steps.  Then u = the principal eigenvector
-//   of X and q = G_pinv P u = G^H (K + a^2 I)^-1 P u.
+//   they run as one device block in f32 like the reference's (MM normalised to a largest entry
+//   of 1), m * 100 steps.  Then u = the principal eigenvector of X and
+//   q = G_pinv P u = G^H (K + a^2 I)^-1 P u.
 //
 //   Long (long.rs:48-105).  X = (amps_i conj(G_ij) / d_i)^T with d = G's row sums, so
 //   R = G X = K diag(amps / d).  The phases e_k = arg V[imax, k] of the eigenvector matrix's
@@ -73,19 +74,17 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
     return v;
 }
 
-// Sum over the block (blockDim.x a multiple of 32, at most 1024); every thread gets the total.
+// Sum over the block (blockDim.x a multiple of 32, at most 1024), valid in thread 0.
 __device__ double2 block_sum2(double2 v, double2* red) {
     v = warp_sum2(v);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    double2 t = make_double2(0.0, 0.0);
-    for (int w = 0; w < nw; ++w) {
-        t.x += red[w].x;
-        t.y += red[w].y;
+    if (warp == 0) {
+        v = lane < nw ? red[lane] : make_double2(0.0, 0.0);
+        v = warp_sum2(v);
     }
-    return t;
+    return v;
 }
 
 // out[i m + k] = sum_j G_ij w_j conj(G_kj) (w = 1 if null) for k <= i, the upper triangle its
@@ -159,48 +158,57 @@ __global__ void backproject_kernel(const float2* __restrict__ g, int64_t n, int 
     q[j] = make_double2(acc.x * s, acc.y * s);
 }
 
-// Horn's SDP by block-coordinate descent (horn.rs:84-117) in one block: x (m x m, row-major,
-// identity on entry) is updated in place, one coordinate idx[t] per step.  Step t with ii =
-// idx[t]: c = column ii of mm without row ii; xb = x' c over the rows and columns other than
-// ii; gamma = Re(xb^H c); row and column ii of x (but not x_ii) become -sqrt(lambda / gamma) xb
-// (its conjugate in the row) if gamma > 0, else zero.
+// Horn's SDP by block-coordinate descent (horn.rs:84-117) in one block, in f32 like the
+// reference: x (m x m, row-major, identity on entry) is updated in place, one coordinate idx[t]
+// per step.  Step t with ii = idx[t]: c = column ii of mm without row ii; xb = x' c over the
+// rows and columns other than ii; gamma = Re(xb^H c); row and column ii of x (but not x_ii)
+// become -sqrt(lambda / gamma) xb (its conjugate in the row) if gamma > 0, else zero.  The
+// steps are invariant to the scale of mm, which the host normalises to a largest entry of 1.
 __global__ void __launch_bounds__(kHornThreads)
-horn_sdp_kernel(int m, const double2* __restrict__ mm, const int* __restrict__ idx,
-                int64_t steps, double lambda, double2* __restrict__ x) {
-    extern __shared__ double2 sh[];
-    double2* col = sh;       // m: column ii of mm, 0 at ii
-    double2* xb = sh + m;    // m: x' c, 0 at ii
-    double2* red = sh + 2 * m;  // 32
+horn_sdp_kernel(int m, const float2* __restrict__ mm, const int* __restrict__ idx,
+                int64_t steps, float lambda, float2* __restrict__ x) {
+    extern __shared__ float2 shf[];
+    float2* col = shf;     // m: column ii of mm, 0 at ii
+    float2* xb = shf + m;  // m: x' c, 0 at ii
+    __shared__ float s_scale;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int64_t t = 0; t < steps; ++t) {
         const int ii = idx[t];
         for (int r = threadIdx.x; r < m; r += blockDim.x)
-            col[r] = r == ii ? make_double2(0.0, 0.0) : mm[static_cast<int64_t>(r) * m + ii];
+            col[r] = r == ii ? make_float2(0.f, 0.f) : mm[static_cast<int64_t>(r) * m + ii];
         __syncthreads();
         for (int r = warp; r < m; r += nw) {
-            double2 acc = make_double2(0.0, 0.0);
+            float2 acc = make_float2(0.f, 0.f);
             if (r != ii) {
-                const double2* xr = x + static_cast<int64_t>(r) * m;
+                const float2* xr = x + static_cast<int64_t>(r) * m;
                 for (int c = lane; c < m; c += 32) {
-                    const double2 a = xr[c], b = col[c];
-                    acc.x += a.x * b.x - a.y * b.y;
-                    acc.y += a.x * b.y + a.y * b.x;
+                    const float2 a = xr[c], b = col[c];
+                    acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
+                    acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
                 }
-                acc = warp_sum2(acc);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+                    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+                }
             }
             if (lane == 0) xb[r] = acc;
         }
         __syncthreads();
-        // gamma = Re(sum_r conj(xb_r) c_r), the same in every thread
-        double2 gp = make_double2(0.0, 0.0);
-        for (int r = threadIdx.x; r < m; r += blockDim.x) gp.x += xb[r].x * col[r].x + xb[r].y * col[r].y;
-        const double gamma = block_sum2(gp, red).x;
-        const double sc = gamma > 0.0 ? -sqrt(lambda / gamma) : 0.0;
+        if (warp == 0) {  // gamma = Re(sum_r conj(xb_r) c_r)
+            float gp = 0.f;
+            for (int r = lane; r < m; r += 32) gp = fmaf(xb[r].x, col[r].x, fmaf(xb[r].y, col[r].y, gp));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) gp += __shfl_xor_sync(0xffffffffu, gp, o);
+            if (lane == 0) s_scale = gp > 0.f ? -sqrtf(lambda / gp) : 0.f;
+        }
+        __syncthreads();
+        const float sc = s_scale;
         for (int r = threadIdx.x; r < m; r += blockDim.x) {
             if (r == ii) continue;
-            const double2 v = make_double2(xb[r].x * sc, xb[r].y * sc);
+            const float2 v = make_float2(xb[r].x * sc, xb[r].y * sc);
             x[static_cast<int64_t>(r) * m + ii] = v;
-            x[static_cast<int64_t>(ii) * m + r] = make_double2(v.x, -v.y);
+            x[static_cast<int64_t>(ii) * m + r] = make_float2(v.x, -v.y);
         }
         __syncthreads();
     }
@@ -345,27 +353,41 @@ int solve_matrix(int kind, int st, float* src, const float* k, const float* atte
             *err = std::string(name) + ": G G^H + a^2 I is not positive definite";
             return -1;
         }
-        std::vector<cd> mmat(mm), x0(mm, cd(0.0, 0.0));
-        for (int i = 0; i < mi; ++i) {
-            x0[i * mi + i] = 1.0;
-            for (int c = 0; c < mi; ++c)
+        // MM in f32, scaled to a largest |re| or |im| of 1 (the SDP steps do not see the scale)
+        std::vector<cd> mmat(mm);
+        double mmax = 0.0;
+        for (int i = 0; i < mi; ++i)
+            for (int c = 0; c < mi; ++c) {
                 mmat[i * mi + c] = a2 * static_cast<double>(amps[i]) * ainv[i * mi + c] *
                                    static_cast<double>(amps[c]);
+                mmax = std::max(mmax, std::max(std::fabs(mmat[i * mi + c].real()),
+                                               std::fabs(mmat[i * mi + c].imag())));
+            }
+        if (!(mmax > 0.0) || !std::isfinite(mmax)) {
+            *err = std::string(name) + ": the SDP matrix is zero or not finite";
+            return -1;
         }
+        std::vector<float> mmf(2 * mm), xf(2 * mm, 0.f);
+        for (size_t i = 0; i < mm; ++i) {
+            mmf[2 * i] = static_cast<float>(mmat[i].real() / mmax);
+            mmf[2 * i + 1] = static_cast<float>(mmat[i].imag() / mmax);
+        }
+        for (int i = 0; i < mi; ++i) xf[2 * (static_cast<size_t>(i) * mi + i)] = 1.f;
         const std::vector<int> idx = horn_indices(mi, steps);
-        const std::vector<double> mmh = from_cd(mmat), xh = from_cd(x0);
-        if ((e = cudaMemcpyAsync(d + o_kk, mmh.data(), 16 * mm, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(d + o_x, xh.data(), 16 * mm, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        if ((e = cudaMemcpyAsync(d + o_kk, mmf.data(), 8 * mm, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(d + o_x, xf.data(), 8 * mm, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
             (e = cudaMemcpyAsync(d + o_idx, idx.data(), 4 * steps, cudaMemcpyHostToDevice, s)) != cudaSuccess)
             return fail("upload MM");
-        const size_t shm = (2 * static_cast<size_t>(m) + 32) * sizeof(double2);
-        horn_sdp_kernel<<<1, kHornThreads, shm, s>>>(mi, D2(o_kk), reinterpret_cast<int*>(d + o_idx),
-                                                     steps, kHornLambda, D2(o_x));
+        const size_t shm = 2 * static_cast<size_t>(m) * sizeof(float2);
+        horn_sdp_kernel<<<1, kHornThreads, shm, s>>>(mi, F2(o_kk), reinterpret_cast<int*>(d + o_idx),
+                                                     steps, static_cast<float>(kHornLambda), F2(o_x));
         count_launch();
+        std::vector<float> xo(2 * mm);
         if ((e = cudaGetLastError()) != cudaSuccess ||
-            (e = cudaMemcpyAsync(h.data(), d + o_x, 16 * mm, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(xo.data(), d + o_x, 8 * mm, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
             return fail("SDP");
+        for (size_t i = 0; i < 2 * mm; ++i) h[i] = xo[i];
         // horn.rs:119-121: u = principal eigenvector of X; q = G_pinv P u = G^H (K + a^2 I)^-1 P u
         std::vector<cd> xm = to_cd(h), v;
         std::vector<double> lam;

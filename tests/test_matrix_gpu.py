@@ -8,6 +8,8 @@ the foci.  Both results depend on how the eigenvectors are ordered and phased (L
 phases come from every eigenvector, Horn's amplitude scale from camax of its phased drive); the
 library and the oracle share one convention (ascending eigenvalues, first nonzero entry real
 and positive), so the drives are compared as they are."""
+import time
+
 import numpy as np
 import pytest
 
@@ -44,7 +46,9 @@ def test_horn_matches_f64(gpu, m):
     rng = np.random.default_rng(600 + m)
     w, foci, amps = W.gspat_request(rng, m)
     s = _system(afc, w)
+    t0 = time.perf_counter()
     afc.Optimizer.horn(s, foci, amps)
+    print(f"Horn m={m}: {1e3 * (time.perf_counter() - t0):.1f} ms")
     got = s.records().copy()
     ref_src, _ = O.horn_f64(1, w.sources, w.k, w.atten, foci, amps)
     e, ef = _compare("Horn", m, got, ref_src, w, foci)
@@ -59,7 +63,9 @@ def test_long_matches_f64(gpu, m):
     rng = np.random.default_rng(700 + m)
     w, foci, amps = W.gspat_request(rng, m)
     s = _system(afc, w)
+    t0 = time.perf_counter()
     afc.Optimizer.long2014(s, foci, amps)
+    print(f"Long m={m}: {1e3 * (time.perf_counter() - t0):.1f} ms")
     got = s.records().copy()
     ref_src, _ = O.long_f64(1, w.sources, w.k, w.atten, foci, amps)
     e, ef = _compare("Long", m, got, ref_src, w, foci)
