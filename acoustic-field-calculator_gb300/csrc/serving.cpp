@@ -184,10 +184,11 @@ class Engine {
     }
 
     // ---- work of one request on its slot's stream
-    cudaError_t launch(Request& r) {
+    // g: the request's geometry, looked up under `mu` (a deque element stays where it is while
+    // geometries are added, but the lookup itself must not race with an addition).
+    cudaError_t launch(Request& r, const Geometry& g) {
         Slot& sl = slots[r.slot];
         cudaStream_t s = sl.stream;
-        const Geometry& g = geoms[r.geom];
         char* d = d_arena + r.d_off;
         char* h = h_arena + r.h_off;
         cudaError_t e;
@@ -281,11 +282,13 @@ class Engine {
             }
             for (int64_t id : to_launch) {
                 Request* r;
+                const Geometry* g;
                 {
                     std::lock_guard<std::mutex> lk(mu);
                     r = &reqs[id];
+                    g = &geoms[r->geom];
                 }
-                const cudaError_t e = launch(*r);
+                const cudaError_t e = launch(*r, *g);
                 if (e != cudaSuccess) {
                     std::lock_guard<std::mutex> lk(mu);
                     r->error = cudaGetErrorString(e);
@@ -497,13 +500,16 @@ extern "C" int64_t AFC_ServeSubmitField(void* engine, int32_t geometry, const fl
                                         const AfcGridDesc* grid, const float* h_points,
                                         uint64_t n_points, float* h_out) {
     Engine* e = static_cast<Engine*>(engine);
-    if (!e || geometry < 0 || geometry >= static_cast<int32_t>(e->geoms.size()) ||
-        field_type < FIELD_PRESSURE || field_type > FIELD_COMPLEX || !h_out) {
+    int64_t gn = -1;  // the geometry's source count, read under the lock AddGeometry takes
+    if (e && geometry >= 0) {
+        std::lock_guard<std::mutex> lk(e->mu);
+        if (geometry < static_cast<int32_t>(e->geoms.size())) gn = e->geoms[geometry].n;
+    }
+    if (!e || gn < 0 || field_type < FIELD_PRESSURE || field_type > FIELD_COMPLEX || !h_out) {
         set_error_message("AFC_ServeSubmitField: invalid argument");
         return AFC_ERR_INVALID;
     }
-    const Geometry& g = e->geoms[geometry];
-    if (g.n && (!h_amps || !h_phases)) {
+    if (gn && (!h_amps || !h_phases)) {
         set_error_message("AFC_ServeSubmitField: amplitudes / phases are NULL");
         return AFC_ERR_INVALID;
     }
@@ -526,7 +532,7 @@ extern "C" int64_t AFC_ServeSubmitField(void* engine, int32_t geometry, const fl
         r.ps.grid.count[0] = r.ps.grid.count[1] = r.ps.grid.count[2] = 1;
         r.ps.m = static_cast<int64_t>(n_points);
     }
-    const int64_t n = g.n, m = r.ps.m;
+    const int64_t n = gn, m = r.ps.m;
     r.out_bytes = field_elem_bytes(field_type) * static_cast<size_t>(m);
     r.user_out = h_out;
     const size_t pts_bytes = is_grid ? 0 : 12 * static_cast<size_t>(m);
@@ -545,13 +551,16 @@ extern "C" int64_t AFC_ServeSubmitGspat(void* engine, int32_t geometry, const fl
                                         const AfcGridDesc* slice, float* h_slice_out,
                                         float* h_amp_phase_out) {
     Engine* e = static_cast<Engine*>(engine);
-    if (!e || geometry < 0 || geometry >= static_cast<int32_t>(e->geoms.size()) ||
-        n_foci == 0 || !h_foci || !h_amps || !h_slice_out ||
+    int64_t gn = -1;  // the geometry's source count, read under the lock AddGeometry takes
+    if (e && geometry >= 0) {
+        std::lock_guard<std::mutex> lk(e->mu);
+        if (geometry < static_cast<int32_t>(e->geoms.size())) gn = e->geoms[geometry].n;
+    }
+    if (!e || gn < 0 || n_foci == 0 || !h_foci || !h_amps || !h_slice_out ||
         n_foci > static_cast<uint64_t>(kSolverMaxFoci)) {
         set_error_message("AFC_ServeSubmitGspat: invalid argument");
         return AFC_ERR_INVALID;
     }
-    const Geometry& g = e->geoms[geometry];
     Request r;
     r.kind = KIND_GSPAT;
     r.geom = geometry;
@@ -562,7 +571,7 @@ extern "C" int64_t AFC_ServeSubmitGspat(void* engine, int32_t geometry, const fl
         return AFC_ERR_INVALID;
     }
     r.ps.m = r.ps.grid.count[0] * r.ps.grid.count[1] * r.ps.grid.count[2];
-    const int64_t n = g.n, M = r.n_foci;
+    const int64_t n = gn, M = r.n_foci;
     r.out_bytes = 4 * static_cast<size_t>(r.ps.m);
     r.out2_bytes = 8 * static_cast<size_t>(n);
     r.user_out = h_slice_out;
