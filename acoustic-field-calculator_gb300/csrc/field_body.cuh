@@ -73,7 +73,7 @@ __device__ __forceinline__ void load_dir_tables(SmemTile& sm, const float4* __re
 // source of a tile and every point of the block: the approximations take their argument in
 // turns after one FP32 multiply, whose rounding gives an absolute error of ~1.2e-7 |phase|
 // (<= 8e-5 rad here, the order of the reference's own f32 rounding of phi + k r); larger
-// phases are first reduced to [-pi, pi] (reduce_phase2).
+// phases are first reduced to [-pi, pi] (ref_phase2).
 constexpr float kUnreducedPhaseMax = 640.0f;
 
 // Neumaier's compensated addition: sum + v with the lost low-order part added to comp.
@@ -118,13 +118,38 @@ __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); 
 __device__ __forceinline__ float& lane_of(float2& v, int hi) { return hi ? v.y : v.x; }
 __device__ __forceinline__ float lane_of(const float2& v, int hi) { return hi ? v.y : v.x; }
 
-// Reduced phase phi + k r - n 2pi in [-pi, pi] for two points, with 2 pi rounded to f32:
-// the reduction error n (2 pi - float(2 pi)) is below 1.2e-5 rad for n < 70 turns (distances
-// up to ~600 mm at 40 kHz), comparable to the rounding of phi + k r itself in the reference.
-__device__ __forceinline__ float2 reduce_phase2(float2 k, float2 r, float2 phase) {
-    const float2 ph = fma2(k, r, phase);
+// The far tiles' phase, rounded as the reference rounds it (uniform_medium.rs:111-120): from
+// q2 = (dx dx + dy dy) + dz dz summed in x, y, z order without contraction, dist = sqrt(q2)
+// rounded to nearest, phi = phase + k dist with the product and the sum rounded separately;
+// then reduced to [-pi, pi] with 2 pi in two parts (Cody and Waite: n kTwoPiHi leaves the FMA
+// unrounded and n kTwoPiLo corrects float(2 pi), whose error would add 1.7e-7 rad per turn).
+// At distances of metres the reference's own f32 rounding of phi (1e-4 rad at 3 m) is as large
+// as the field bar, so a phase rounded any other way would differ from its field by about that
+// much.  A source with a negative amplitude carries phase + pi (PackedSource), whose rounding
+// differs.
+//
+// dist (returned in r) is q2 rinv with one Newton step (refine_r), rinv ~ rsqrt(q2) (the pair's
+// rsqrt.approx of its own r^2 is close enough): over 2e6 pairs at 1.5 to 6 m it equalled the
+// IEEE square root every time.  sqrt.rn itself is not used because any call of it in these
+// kernels, even on a path the launch never takes, cost the near-field loop 1-2 %.  The products
+// and sums are the scalar __fmul_rn / __fadd_rn, which are never merged into an FMA: with the
+// packed forms the far-field test measured the fused rounding of phase + k dist (1.3e-4 of the
+// peak at 3 m, against 3e-6 for the reference's rounding).
+__device__ __forceinline__ float2 ref_phase2(float2 q2, float2 rinv, float2 k, float2 phase,
+                                             float2& r) {
+    r = make_float2(refine_r(q2.x, rinv.x, q2.x * rinv.x), refine_r(q2.y, rinv.y, q2.y * rinv.y));
+    const float2 ph = make_float2(__fadd_rn(phase.x, __fmul_rn(k.x, r.x)),
+                                  __fadd_rn(phase.y, __fmul_rn(k.y, r.y)));
     const float2 nq = add2(fma2(ph, f2(kInv2Pi), f2(kRoundMagic)), f2(-kRoundMagic));
-    return fma2(nq, f2(-kTwoPiHi), ph);
+    return fma2(nq, f2(-kTwoPiLo), fma2(nq, f2(-kTwoPiHi), ph));
+}
+
+// (dx dx + dy dy) + dz dz rounded after every operation, for one point.
+__device__ __forceinline__ float ref_dist2_1(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+__device__ __forceinline__ float2 ref_dist2(float2 dx, float2 dy, float2 dz) {
+    return make_float2(ref_dist2_1(dx.x, dy.x, dz.x), ref_dist2_1(dx.y, dy.y, dz.y));
 }
 
 // Correction for one point of a thread whose points include one next to a bin edge: recompute
@@ -158,9 +183,10 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
     const int i_fast = fast_bin(thc);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
     if (i_exact == i_fast) return make_float2(0.f, 0.f);
-    const float r = r2 * rinv;
-    const float w0 = rinv * mufu_ex2(fmaf(v3.z, r, v4.x));
-    const float red = reduce_phase2(f2(v1.z), f2(r), f2(v4.z)).x;
+    float2 r;
+    const float red =
+        ref_phase2(ref_dist2(f2(dx), f2(dy), f2(dz)), f2(rinv), f2(v1.z), f2(v4.z), r).x;
+    const float w0 = rinv * mufu_ex2(fmaf(v3.z, r.x, v4.x));
     const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - dir_in_bin(tab, thc, i_fast));
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
@@ -186,8 +212,9 @@ struct PairGeom {
 // records whether any of the thread's points has its theta next to a bin edge; that rare case
 // recomputes the pairs' geometry to find which points, and corrects them one by one.  RED:
 // the careful variant, for tiles with a large phase bound or with some point possibly behind a
-// source: the phase is reduced before sin/cos (see kUnreducedPhaseMax), and a cos(theta) next
-// to -1 (kBackAxisC) also takes the exact path.  This body keeps the theta-binned
+// source: the phase is rounded as the reference rounds it and reduced before sin/cos
+// (ref_phase2, kUnreducedPhaseMax), and a cos(theta) next to -1 (kBackAxisC) also takes the
+// exact path.  This body keeps the theta-binned
 // directivity (acos polynomial and MUFU square root): with three coordinates per point it has
 // no registers left for the cos(theta)-indexed table's two dependent lookups, which spill here
 // and made the batched kernel 12 % slower, while the rows body (field_rows.cuh) gains 8 %.
@@ -208,7 +235,11 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
-        const float2 r = mul2(p.r2, p.rinv);
+        float2 r = mul2(p.r2, p.rinv);
+        float2 red;
+        if constexpr (RED)
+            red = ref_phase2(ref_dist2(p.dx, p.dy, p.dz), p.rinv, hi2(v1), hi2(v4), r);
+        else red = fma2(hi2(v1), r, hi2(v4));
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
@@ -217,7 +248,6 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
             any_near |= near_edge(xc.x) | near_edge(xc.y);
             if constexpr (RED) any_near |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
         }
-        const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
         const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
         if constexpr (SUM == SUM_PLAIN) {

@@ -30,10 +30,28 @@ __device__ __forceinline__ float pick3(float x, float y, float z, int a) {
 }
 
 // Per thread and source: offsets along the grid's first (v) and third (w) axes, v^2 + w^2,
-// and n_v v + n_w w.
+// and n_v v + n_w w; for the far tiles also qb, qc with which the reference's
+// (dx dx + dy dy) + dz dz is (du du + qb) + qc in the same rounding (see row_q2_parts).
 struct RowShared {
-    float dv, dw, vw2, nvw;
+    float dv, dw, vw2, nvw, qb, qc;
 };
+
+// The reference sums the squared offsets in x, y, z order (uniform_medium.rs:111-113); the rows
+// body has the second grid axis's (u) per pair and the others' per source.  With a1 the xyz
+// index of u and a0 that of v: u = z gives (du du + (sx + sy)) + 0, u = x gives
+// (du du + sy) + sz and u = y gives (du du + sx) + sz, each rounding as the reference's sum
+// (an addition commutes exactly, and adding +0 to a non-negative sum changes nothing).
+__device__ __forceinline__ void row_q2_parts(float dv, float dw, int a0, int a1, float& qb,
+                                             float& qc) {
+    const float sv = __fmul_rn(dv, dv), sw = __fmul_rn(dw, dw);
+    if (a1 == 2) {
+        qb = __fadd_rn(sv, sw);
+        qc = 0.f;
+    } else {
+        qb = a1 == 0 ? (a0 == 1 ? sv : sw) : (a0 == 0 ? sv : sw);  // y for u = x, x for u = y
+        qc = a0 == 2 ? sv : sw;                                      // z
+    }
+}
 
 // Point pair q of a thread against the staged source: offset along the second axis, r^2, 1/r,
 // the numerator of cos(theta) and cos(theta), with the same operations on the hot loop and on
@@ -77,9 +95,10 @@ static __device__ __noinline__ float2 edge_correction_rows(const float4* __restr
     const float ny = a0 == 1 ? n_a0 : (a1 == 1 ? n_a1 : n_a2);
     const float nz = a0 == 2 ? n_a0 : (a1 == 2 ? n_a1 : n_a2);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
-    const float r = r2 * rinv;
-    const float w0 = rinv * mufu_ex2(fmaf(a2c, r, la));
-    const float red = reduce_phase2(f2(k), f2(r), f2(phase)).x;
+    float2 r;
+    const float red =
+        ref_phase2(ref_dist2(f2(dx), f2(dy), f2(dz)), f2(rinv), f2(k), f2(phase), r).x;
+    const float w0 = rinv * mufu_ex2(fmaf(a2c, r.x, la));
     const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - d_fast);
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
@@ -108,11 +127,22 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
     sh.vw2 = fmaf(sh.dw, sh.dw, sh.dv * sh.dv);
     sh.nvw = 0.f;
     if constexpr (ST == SRC_T4010A1 && !UD) sh.nvw = fmaf(v3.x, sh.dw, v2.x * sh.dv);
+    sh.qb = sh.qc = 0.f;
+    if constexpr (RED) row_q2_parts(sh.dv, sh.dw, a0, a1, sh.qb, sh.qc);
     float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const RowGeom<UD> p(U[q], NP[q], sh, v0, v2, ns);
-        const float2 r = mul2(p.r2, p.rinv);
+        float2 r = mul2(p.r2, p.rinv);
+        float2 red;
+        if constexpr (RED) {
+            const float2 q2 =
+                make_float2(__fadd_rn(__fadd_rn(__fmul_rn(p.du.x, p.du.x), sh.qb), sh.qc),
+                            __fadd_rn(__fadd_rn(__fmul_rn(p.du.y, p.du.y), sh.qb), sh.qc));
+            red = ref_phase2(q2, p.rinv, hi2(v1), hi2(v4), r);
+        } else {
+            red = fma2(hi2(v1), r, hi2(v4));
+        }
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
@@ -120,7 +150,6 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
             w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
             near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
         }
-        const float2 red = RED ? reduce_phase2(hi2(v1), r, hi2(v4)) : fma2(hi2(v1), r, hi2(v4));
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
         const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
         if constexpr (SUM == SUM_PLAIN) {

@@ -160,6 +160,14 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+// r = sqrt(r2) from r0 = r2 * rsqrt.approx(r2) and one Newton step, r0 + (r2 - r0^2) / (2 r0)
+// with 1 / r0 ~ rinv: the approximation's relative error (~1.3e-7) would otherwise turn into a
+// phase error k r 1.3e-7 that grows with distance (2e-4 rad at 3 m, 40 kHz).  Used by the
+// transfer-matrix builds and by the field kernels' far tiles.
+__device__ __forceinline__ float refine_r(float r2, float rinv, float r0) {
+    return fmaf(0.5f * fmaf(-r0, r0, r2), rinv, r0);
+}
+
 // ------------------------------------------------------------------ directivity
 
 // The reference's bin for one pair (uniform_medium.rs:113-116, t4010a1.rs:107-120): its f32
@@ -315,7 +323,7 @@ __device__ __forceinline__ void pair_terms(const float4& a, const float4& b, flo
     const float dz = pz - a.z;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float rinv = mufu_rsqrt(r2);
-    const float r = r2 * rinv;
+    const float r = refine_r(r2, rinv, r2 * rinv);
     w = rinv * mufu_ex2(fmaf(b.w, r, la));
     if constexpr (ST == SRC_T4010A1) {
         const float ct = fmaf(b.z, dz, fmaf(b.y, dy, b.x * dx)) * rinv;
