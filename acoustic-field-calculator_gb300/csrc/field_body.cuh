@@ -132,9 +132,11 @@ __device__ __forceinline__ float lane_of(const float2& v, int hi) { return hi ? 
 // rsqrt.approx of its own r^2 is close enough): over 2e6 pairs at 1.5 to 6 m it equalled the
 // IEEE square root every time.  sqrt.rn itself is not used because any call of it in these
 // kernels, even on a path the launch never takes, cost the near-field loop 1-2 %.  The products
-// and sums are the scalar __fmul_rn / __fadd_rn, which are never merged into an FMA: with the
-// packed forms the far-field test measured the fused rounding of phase + k dist (1.3e-4 of the
-// peak at 3 m, against 3e-6 for the reference's rounding).
+// and sums are the scalar __fmul_rn / __fadd_rn, which are never merged into an FMA.  A packed
+// product feeding a packed sum is not safe from that: on 1M random inputs __fmul2_rn then
+// __fadd2_rn, and equally mul.rn.f32x2 then add.rn.f32x2 written in PTX, gave the fused result
+// wherever it differs (261,351 cases), and the far-field test measured the fused rounding of
+// phase + k dist (1.3e-4 of the peak at 3 m, against 3e-6 for the reference's rounding).
 __device__ __forceinline__ float2 ref_phase2(float2 q2, float2 rinv, float2 k, float2 phase,
                                              float2& r) {
     r = make_float2(refine_r(q2.x, rinv.x, q2.x * rinv.x), refine_r(q2.y, rinv.y, q2.y * rinv.y));
