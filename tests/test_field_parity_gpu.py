@@ -372,6 +372,54 @@ def test_far_phases_take_the_reduced_path(gpu, layout):
         assert rel_err(out, O.field_f64(1, rec, k, a, p)) <= TOL
 
 
+def test_grid_beyond_2_31_points(gpu):
+    """A 2048 x 2048 x 513 grid (2,151,677,952 points, past 2^31) through the device entry
+    point, pressure kept on the device (8.6 GB): every point index is 64-bit.  4,096 sampled
+    points, among them the last one and the ones past 2^31, match the oracle."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    rng = np.random.default_rng(2 ** 31 % 1000)
+    rec, k, a = random_sources(rng, 1, 3)
+    counts, res = (2048, 2048, 513), 0.5
+    lo0 = (-512.0, -512.0, 40.0)
+    g = W.GridSpec(3, [(lo0[j], lo0[j] + (counts[j] - 0.75) * res) for j in range(3)], res,
+                   (1, 2, 3))
+    area = afc.grid_from_spec(g)
+    desc = area.grid_desc()
+    assert tuple(int(c) for c in desc.count) == counts
+    m = counts[0] * counts[1] * counts[2]
+    assert m > 2 ** 31
+    d_src = torch.from_numpy(rec.reshape(-1)).cuda()
+    d_k = torch.from_numpy(k).cuda()
+    d_a = torch.from_numpy(a).cuda()
+    ws_bytes = afc.DLL.AFC_FieldWorkspaceBytes(len(k))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty(m, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = afc.DLL.AFC_FieldGridDevice(1, 0, 0, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                     len(k), ctypes.byref(desc), out.data_ptr(), ws.data_ptr(),
+                                     ws_bytes, stream)
+    assert rc == 0, afc.last_error()
+    torch.cuda.synchronize()
+    idx = np.concatenate([rng.integers(0, m, 4000), np.arange(2 ** 31 - 40, 2 ** 31 + 40),
+                          np.arange(m - 16, m)]).astype(np.int64)
+    got = out[torch.from_numpy(idx).cuda()].cpu().numpy()
+    del out
+    torch.cuda.empty_cache()
+    i0 = idx % counts[0]
+    i1 = (idx // counts[0]) % counts[1]
+    i2 = idx // (counts[0] * counts[1])
+    lo, _ = g.lo_hi()
+    # o + (i as f32 * res), as the reference generates grid points
+    pts = np.stack([lo[0] + (i0.astype(np.float32) * np.float32(res)),
+                    lo[1] + (i1.astype(np.float32) * np.float32(res)),
+                    lo[2] + (i2.astype(np.float32) * np.float32(res))], 1).astype(np.float32)
+    ref = np.abs(O.field_f32(1, rec, k, a, pts))
+    err = rel_err(got, ref)
+    print(f"2^31+ grid: {m} points, sampled rel err {err:.2e}")
+    assert err <= TOL
+
+
 @pytest.mark.parametrize("dist", [1500.0, 3000.0])
 def test_far_field_with_random_phases(gpu, dist):
     """Every point 1.5 or 3 m from a 4 x 4 tiling (3,984 sources) driven with random phases,
