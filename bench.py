@@ -48,9 +48,9 @@ UNIT = "evals/s"
 MUFU_PER_EVAL = 5
 FP32_PER_EVAL = 32
 # DRAM bytes (read + write) of one 256^3 launch of the field kernel, from an ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum (3.59 MB + 76.80 MB; part of the 134 MB output
+# dram__bytes_read.sum + dram__bytes_write.sum (3.55 MB + 75.95 MB; part of the 134 MB output
 # is still in L2 when the launch ends)
-FIELD_TRAFFIC_256 = 80.39e6
+FIELD_TRAFFIC_256 = 79.50e6
 
 
 def parse():
