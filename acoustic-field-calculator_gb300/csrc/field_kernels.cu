@@ -60,33 +60,24 @@ __global__ void __launch_bounds__(kThreads, 2)
     block_points<ST, SUM, PAIRS>(sm, src, n, GRID, g, pts, m, first, field, out);
 }
 
-// Small launches: a cluster of S blocks per point tile, block rank r summing sources
-// [r c, (r + 1) c), c = ceil(n / S); rank 0 adds ranks 1 .. S-1's partial sums (read from their
-// shared memory through the cluster) in rank order, then stores.  Both cluster barriers are
-// reached by every thread of every block.
-template <int ST, int SUM, bool GRID, int PAIRS>
-__global__ void __launch_bounds__(kThreads, 2)
-    field_split_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
-                       const float* __restrict__ pts, int64_t m, int field,
-                       void* __restrict__ out) {
+// The partial sums of a cluster's blocks, combined into rank 0's: every rank writes its sums
+// into its own staging arrays (free once its last tile is done), rank 0 adds ranks 1 .. S-1's
+// (read from their shared memory through the cluster) in rank order.  Both cluster barriers
+// are reached by every thread of every block; the second keeps the other ranks' shared memory
+// alive until rank 0 has read it.
+template <int SUM, int PAIRS>
+__device__ __forceinline__ void cluster_combine(SmemTile& sm, float2 (&RE)[PAIRS],
+                                                float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                                float2 (&CIM)[PAIRS]) {
     namespace cg = cooperative_groups;
-    __shared__ SmemTile sm;
     constexpr int kPPT = 2 * PAIRS;
     // partial sums (and compensations) of every thread, in the staging arrays once free
     static_assert(sizeof(float2) * (SUM == SUM_COMPENSATED ? 2 : 1) * kPPT * kThreads <=
                       4 * sizeof(sm.v0),
                   "partial sums must fit in the first four staging arrays");
-    load_dir_tables(sm, c_dir_table);
     cg::cluster_group cluster = cg::this_cluster();
     const unsigned S = cluster.num_blocks();
     const unsigned rank = cluster.block_rank();
-    const int64_t first = static_cast<int64_t>(blockIdx.x / S) * (kThreads * kPPT);
-    const int64_t chunk = (n + S - 1) / S;
-    const int64_t s_lo = static_cast<int64_t>(rank) * chunk < n ? static_cast<int64_t>(rank) * chunk : n;
-    const int64_t s_hi = s_lo + chunk < n ? s_lo + chunk : n;
-    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    block_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, GRID, g, pts, m, first, RE, IM, CRE,
-                                     CIM);
     __syncthreads();  // the staging arrays are free
     float2* part = reinterpret_cast<float2*>(sm.v0);
 #pragma unroll
@@ -117,8 +108,61 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
         }
     }
-    cluster.sync();  // the other ranks' shared memory stays alive until rank 0 has read it
-    if (rank == 0) block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
+    cluster.sync();
+}
+
+// Source range [r c, (r + 1) c) of rank r of S, c = ceil(n / S).
+__device__ __forceinline__ void rank_sources(int64_t n, int64_t& s_lo, int64_t& s_hi) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int64_t S = cluster.num_blocks(), rank = cluster.block_rank();
+    const int64_t chunk = (n + S - 1) / S;
+    s_lo = rank * chunk < n ? rank * chunk : n;
+    s_hi = s_lo + chunk < n ? s_lo + chunk : n;
+}
+
+// Small launches: a cluster of S blocks per point tile, block rank r summing its share of the
+// sources (rank_sources); rank 0 combines the partial sums (cluster_combine) and stores.
+template <int ST, int SUM, bool GRID, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_split_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                       const float* __restrict__ pts, int64_t m, int field,
+                       void* __restrict__ out) {
+    namespace cg = cooperative_groups;
+    __shared__ SmemTile sm;
+    constexpr int kPPT = 2 * PAIRS;
+    load_dir_tables(sm, c_dir_table);
+    const unsigned S = cg::this_cluster().num_blocks();
+    const int64_t first = static_cast<int64_t>(blockIdx.x / S) * (kThreads * kPPT);
+    int64_t s_lo, s_hi;
+    rank_sources(n, s_lo, s_hi);
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    block_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, GRID, g, pts, m, first, RE, IM, CRE,
+                                     CIM);
+    cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
+    if (cg::this_cluster().block_rank() == 0)
+        block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
+}
+
+// Mid-size grids: the rows tiling with every tile's sources split over a cluster of S blocks,
+// S chosen so that the launch fills whole waves (rows_split_width); rank 0 combines and stores.
+template <int ST, int SUM, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_rows_split_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                            int tx_log2, int64_t tiles0, int64_t tiles1, int field,
+                            void* __restrict__ out) {
+    namespace cg = cooperative_groups;
+    __shared__ SmemTile sm;
+    load_dir_tables(sm, c_dir_table);
+    const int64_t tile = blockIdx.x / cg::this_cluster().num_blocks();
+    int64_t s_lo, s_hi;
+    rank_sources(n, s_lo, s_hi);
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    rows_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, g, tx_log2, tiles0, tiles1, tile, RE,
+                                    IM, CRE, CIM);
+    cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
+    if (cg::this_cluster().block_rank() == 0)
+        rows_store<SUM, PAIRS>(g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field, out);
 }
 
 // Grids with more than one point along their second axis: tiles of TX = 1 << tx_log2 first-axis
@@ -146,6 +190,28 @@ int g_num_sms = 0;
 // least kSplitMinSources sources.
 constexpr int64_t kMaxClusterBlocks = 8;
 constexpr int64_t kSplitMinSources = 64;
+
+// Cluster width for a rows launch of `blocks` tiles over n sources on `slots` resident blocks:
+// 1 when the launch fills its last wave to 93 % or more (large grids), else the S <= 8 (each
+// rank keeping >= kSplitMinSources sources) whose blocks * S best fill whole waves, each extra
+// rank charged 1 % for its set-up and the combine.
+int64_t rows_split_width(int64_t blocks, int64_t n, int64_t slots) {
+    auto fill = [&](int64_t b) {
+        const int64_t waves = (b + slots - 1) / slots;
+        return static_cast<double>(b) / static_cast<double>(waves * slots);
+    };
+    if (blocks <= 0 || fill(blocks) >= 0.93) return 1;
+    int64_t best = 1;
+    double best_score = fill(blocks);
+    for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
+        const double score = fill(blocks * S) - 0.01 * static_cast<double>(S - 1);
+        if (score > best_score + 1e-9) {
+            best = S;
+            best_score = score;
+        }
+    }
+    return best;
+}
 
 template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
@@ -187,6 +253,26 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         const RowsTiling t = rows_tiling(ps.grid, ps.m, PAIRS);
         if (t.use) {
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+            const int64_t S = rows_split_width(t.blocks, n, want);
+            if (S >= 2 && t.blocks * S <= 0x7fffffffLL) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(static_cast<unsigned>(t.blocks * S), 1, 1);
+                cfg.blockDim = dim3(kThreads, 1, 1);
+                cfg.dynamicSmemBytes = 0;
+                cfg.stream = s;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = static_cast<unsigned>(S);
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                const cudaError_t e =
+                    cudaLaunchKernelEx(&cfg, field_rows_split_kernel<ST, SUM, PAIRS>, src, n,
+                                       ps.grid, t.tx_log2, t.tiles0, t.tiles1, field, out);
+                count_launch();
+                return e != cudaSuccess ? e : cudaGetLastError();
+            }
             field_rows_kernel<ST, SUM, PAIRS><<<static_cast<unsigned>(t.blocks), kThreads, 0, s>>>(
                 src, n, ps.grid, t.tx_log2, t.tiles0, t.tiles1, field, out);
             count_launch();

@@ -198,12 +198,16 @@ __device__ __forceinline__ float axis_coord(const GridDev& g, int k, int a, int6
     return g.count[k] > 1 ? __fadd_rn(o, __fmul_rn(__ll2float_rn(i), g.res)) : o;
 }
 
-// One tile of the rows tiling (tile index -> (t0, t1) of plane i2; TX = 1 << tx_log2).
+// One tile of the rows tiling (tile index -> (t0, t1) of plane i2; TX = 1 << tx_log2): the sums
+// of sources s_lo .. s_hi - 1 at the thread's points, in RE, IM (CRE, CIM: compensations).
+// Source 0's direction is the shared direction of the fast cos(theta) whatever the range.
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __restrict__ src,
-                                           int64_t n, const GridDev& g, int tx_log2,
-                                           int64_t tiles0, int64_t tiles1, int64_t tile,
-                                           int field, void* __restrict__ out) {
+__device__ __forceinline__ void rows_accumulate(SmemTile& sm, const PackedSource* __restrict__ src,
+                                                int64_t n, int64_t s_lo, int64_t s_hi,
+                                                const GridDev& g, int tx_log2, int64_t tiles0,
+                                                int64_t tiles1, int64_t tile, float2 (&RE)[PAIRS],
+                                                float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                                float2 (&CIM)[PAIRS]) {
     constexpr int kPPT = 2 * PAIRS;
     const int tx = threadIdx.x & ((1 << tx_log2) - 1);
     const int ty = threadIdx.x >> tx_log2;
@@ -216,7 +220,7 @@ __device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __r
     const float p0 = axis_coord(g, 0, a0, i0 < c0 ? i0 : c0 - 1);
     const float p2 = axis_coord(g, 2, a2, i2);
 
-    float2 U[PAIRS], NP[PAIRS], RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    float2 U[PAIRS], NP[PAIRS];
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         const int64_t i1 = i1b + k < c1 ? i1b + k : c1 - 1;  // computed but never stored
@@ -280,8 +284,8 @@ __device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __r
         __syncthreads();
     }
 
-    for (int64_t s0 = 0; s0 < n; s0 += kTile) {
-        const int cnt = static_cast<int>((n - s0) < kTile ? (n - s0) : kTile);
+    for (int64_t s0 = s_lo; s0 < s_hi; s0 += kTile) {
+        const int cnt = static_cast<int>((s_hi - s0) < kTile ? (s_hi - s0) : kTile);
         __syncthreads();
         bool same_dir = true, small_phase = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
@@ -333,6 +337,23 @@ __device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __r
         }
     }
 
+}
+
+// Store the thread's sums of one tile of the rows tiling (field transform applied).
+template <int SUM, int PAIRS>
+__device__ __forceinline__ void rows_store(const GridDev& g, int tx_log2, int64_t tiles0,
+                                           int64_t tiles1, int64_t tile, float2 (&RE)[PAIRS],
+                                           float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                           float2 (&CIM)[PAIRS], int field,
+                                           void* __restrict__ out) {
+    constexpr int kPPT = 2 * PAIRS;
+    const int tx = threadIdx.x & ((1 << tx_log2) - 1);
+    const int ty = threadIdx.x >> tx_log2;
+    const int64_t t0 = tile % tiles0, rest = tile / tiles0;
+    const int64_t t1 = rest % tiles1, i2 = rest / tiles1;
+    const int64_t c0 = g.count[0], c1 = g.count[1];
+    const int64_t i0 = (t0 << tx_log2) + tx;
+    const int64_t i1b = (t1 * (kThreads >> tx_log2) + ty) * kPPT;
     if (i0 >= c0) return;
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
@@ -353,6 +374,18 @@ __device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __r
             reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
         }
     }
+}
+
+// One tile of the rows tiling, all n sources, stored.
+template <int ST, int SUM, int PAIRS>
+__device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __restrict__ src,
+                                           int64_t n, const GridDev& g, int tx_log2,
+                                           int64_t tiles0, int64_t tiles1, int64_t tile,
+                                           int field, void* __restrict__ out) {
+    float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+    rows_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE, IM,
+                                    CRE, CIM);
+    rows_store<SUM, PAIRS>(g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field, out);
 }
 
 }  // namespace fb

@@ -420,6 +420,39 @@ def test_grid_beyond_2_31_points(gpu):
     assert err <= TOL
 
 
+@pytest.mark.parametrize("calc", ["GpuCalculator", "AccurateCalculator"])
+@pytest.mark.parametrize("tilted", [False, True])
+def test_rows_split_mid_size(gpu, calc, tilted):
+    """A 128 x 128 x 40 grid (655,360 points) has 320 rows tiles, half a wave short of filling
+    its second wave, so the launch splits every tile's 996 sources over a cluster of blocks and
+    combines the partial sums in rank order (plain and compensated).  Checked in full against
+    the oracle."""
+    afc = gpu
+    rng = np.random.default_rng(17 + tilted)
+    pos = W.tiled_array(2, 2)
+    n = len(pos)
+    rec = W.t4010a1_records(pos, rng.uniform(0.5, 1.0, n).astype(np.float32),
+                            rng.uniform(0, 2 * np.pi, n).astype(np.float32))
+    if tilted:
+        d = rng.normal(size=(n, 3)) * np.array([0.3, 0.3, 0.0]) + np.array([0, 0, 1.0])
+        rec[:, 3:6] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    k = np.full(n, W.wavenumber(), np.float32)
+    a = np.full(n, 0.0115, np.float32)
+    cen = W.array_center(pos)
+    x0, y0 = float(cen[0]) - 32.0, float(cen[1]) - 32.0
+    g = W.GridSpec(3, [(x0, x0 + 127.25 * 0.5), (y0, y0 + 127.25 * 0.5), (80.0, 80.0 + 39.25 * 0.5)],
+                   0.5, (1, 2, 3))
+    s = make_system(afc, 1, rec, k, a)
+    lo, hi = g.lo_hi()
+    pts = O.grid_points(3, lo, hi, 0.5, (1, 2, 3))
+    assert len(pts) == 128 * 128 * 40
+    out = getattr(afc, calc)().calculate(s, afc.grid_from_spec(g), afc.ComplexPressureFieldBuffer())
+    ref = O.field_f32(1, rec, k, a, pts, accurate=(calc == "AccurateCalculator"))
+    err = rel_err(out, ref)
+    print(f"rows split {calc} tilted={tilted}: {err:.2e}")
+    assert err <= TOL
+
+
 @pytest.mark.parametrize("dist", [1500.0, 3000.0])
 def test_far_field_with_random_phases(gpu, dist):
     """Every point 1.5 or 3 m from a 4 x 4 tiling (3,984 sources) driven with random phases,
