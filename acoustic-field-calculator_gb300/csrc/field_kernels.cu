@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 }
 
 // Mid-size grids: the rows tiling with every tile's sources split over a cluster of S blocks,
-// S chosen so that the launch fills whole waves (rows_split_width); rank 0 combines and stores.
+// S chosen so that the launch fills whole waves (split_width); rank 0 combines and stores.
 template <int ST, int SUM, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
     field_rows_split_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
@@ -191,11 +191,11 @@ int g_num_sms = 0;
 constexpr int64_t kMaxClusterBlocks = 8;
 constexpr int64_t kSplitMinSources = 64;
 
-// Cluster width for a rows launch of `blocks` tiles over n sources on `slots` resident blocks:
-// 1 when the launch fills its last wave to 93 % or more (large grids), else the S <= 8 (each
-// rank keeping >= kSplitMinSources sources) whose blocks * S best fill whole waves, each extra
-// rank charged 1 % for its set-up and the combine.
-int64_t rows_split_width(int64_t blocks, int64_t n, int64_t slots) {
+// Cluster width for a launch of `blocks` point tiles over n sources on `slots` resident
+// blocks: 1 when the launch fills its last wave to 93 % or more (large launches), else the
+// S <= 8 (each rank keeping >= kSplitMinSources sources) whose blocks * S best fill whole
+// waves, each extra rank charged 1 % for its set-up and the combine.
+int64_t split_width(int64_t blocks, int64_t n, int64_t slots) {
     auto fill = [&](int64_t b) {
         const int64_t waves = (b + slots - 1) / slots;
         return static_cast<double>(b) / static_cast<double>(waves * slots);
@@ -219,12 +219,12 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
     const int64_t want = 2LL * num_sms();
-    if (flat_blocks < want && n >= 2 * kSplitMinSources) {
-        // too few blocks to fill the GPU: split each tile's sources over a cluster
-        int64_t S = (want + flat_blocks - 1) / flat_blocks;
-        if (S > kMaxClusterBlocks) S = kMaxClusterBlocks;
-        if (S > n / kSplitMinSources) S = n / kSplitMinSources;
-        if (S >= 2) {
+    const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
+    if (!rows.use) {
+        // flat numbering whose blocks would leave the last wave short (or the GPU part empty):
+        // split each tile's sources over a cluster
+        const int64_t S = split_width(flat_blocks, n, want);
+        if (S >= 2 && flat_blocks * S <= 0x7fffffffLL) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(static_cast<unsigned>(flat_blocks * S), 1, 1);
             cfg.blockDim = dim3(kThreads, 1, 1);
@@ -250,10 +250,10 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         }
     }
     if (ps.is_grid) {
-        const RowsTiling t = rows_tiling(ps.grid, ps.m, PAIRS);
+        const RowsTiling& t = rows;
         if (t.use) {
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-            const int64_t S = rows_split_width(t.blocks, n, want);
+            const int64_t S = split_width(t.blocks, n, want);
             if (S >= 2 && t.blocks * S <= 0x7fffffffLL) {
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3(static_cast<unsigned>(t.blocks * S), 1, 1);
