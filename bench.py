@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--mp-points", type=int, default=262144, help="multipattern: points")
     ap.add_argument("--mp-patterns", type=int, default=1024, help="multipattern: patterns")
     ap.add_argument("--batch-jobs", type=int, default=2048, help="batch: job count")
+    ap.add_argument("--serve-slots", type=int, default=32,
+                    help="serving: requests in flight on the GPU at most")
     return ap.parse_args()
 
 
@@ -603,7 +605,8 @@ def run_serving(args):
     lib = afc.DLL
     lib.AFC_SetDevice(local)
     pool = W.batch_jobs(n_jobs=256)
-    eng = SC.Engine(afc, hbm_budget_bytes=2 << 30, pinned_bytes=2 << 30, max_inflight=32)
+    eng = SC.Engine(afc, hbm_budget_bytes=2 << 30, pinned_bytes=2 << 30,
+                    max_inflight=args.serve_slots)
     gid_of_n = {}
     for jb in pool:
         if jb.n not in gid_of_n:
@@ -714,7 +717,7 @@ def run_serving(args):
             "config": {"workload": "serving_poisson_field70_gspat30", "pool_jobs": len(pool),
                        "gspat_sources": n_g, "gspat_foci": [2, 64], "gspat_iterations": 100,
                        "slice": [201, 201], "hbm_budget_bytes": st["hbm_budget_bytes"],
-                       "max_inflight": 32},
+                       "max_inflight": args.serve_slots},
             "sweep": sweep,
             "engine": {"completed": st["completed"] - st0["completed"], "failed": st["failed"],
                        "peak_inflight": st["peak_inflight"],
