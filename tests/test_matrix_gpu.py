@@ -114,3 +114,39 @@ def test_matrix_optimizer_edge_cases(gpu):
     afc.Optimizer.horn(s, foci, amps)
     rec = s.records()
     assert rec[5, 6] == 0.0 and np.all(rec[np.arange(len(rec)) != 5, 6] > 0)
+
+
+def _sphere_request(rng, m):
+    """The GS-PAT request geometry with sphere sources (D = 1) instead of T4010A1."""
+    w, foci, amps = W.gspat_request(rng, m)
+    rec = W.sphere_records(w.sources[:, :3], w.sources[:, 6], w.sources[:, 7])
+    return rec, w.k, w.atten, foci, amps
+
+
+def _sphere_drive(rec):
+    rec = rec.reshape(-1, 6)
+    return rec[:, 3].astype(np.float64) * np.exp(1j * rec[:, 4].astype(np.float64))
+
+
+@pytest.mark.parametrize("solver", ["gs_pat", "horn", "long2014"])
+def test_solvers_with_sphere_sources(gpu, solver):
+    """GS-PAT, Horn and Long on sphere sources (source type 0: D = 1, amplitude and phase in
+    fields 3 and 4 of the record) against the float64 oracles, 996 sources, 16 foci."""
+    afc = gpu
+    rng = np.random.default_rng({"gs_pat": 901, "horn": 902, "long2014": 903}[solver])
+    rec, k, a, foci, amps = _sphere_request(rng, 16)
+    s = afc.UniformSystem(300.0)
+    s.add_records(0, rec, k, a)
+    getattr(afc.Optimizer, solver)(s, foci, amps)
+    got = s.records().copy()
+    oracle_fn = {"gs_pat": O.gspat_f64, "horn": O.horn_f64, "long2014": O.long_f64}[solver]
+    ref_src, _ = oracle_fn(0, rec, k, a, foci, amps)
+    d_gpu, d_ref = _sphere_drive(got), _sphere_drive(ref_src)
+    e = np.max(np.abs(d_gpu - d_ref)) / np.max(np.abs(d_ref))
+    p_gpu = np.abs(O.field_f64(0, got, k, a, foci))
+    p_ref = np.abs(O.field_f64(0, ref_src.reshape(-1, 6), k, a, foci))
+    ef = np.max(np.abs(p_gpu - p_ref)) / np.max(p_ref)
+    print(f"{solver} sphere: max |dd|/max|d| = {e:.2e}, focus amplitude err {ef:.2e}")
+    assert e <= 1e-3
+    assert ef <= 1e-3
+    np.testing.assert_array_equal(got[:, [0, 1, 2, 5]], rec[:, [0, 1, 2, 5]])
