@@ -16,13 +16,13 @@ pytestmark = pytest.mark.gpu
 BF16X3, FP16 = 1, 2
 
 
-def _problem(seed, n_tiles, m, K):
+def _problem(seed, n_tiles, m, K, st=1):
     rng = np.random.default_rng(seed)
     pos = W.tiled_array(*n_tiles)
     cen = W.array_center(pos)
     pts = W.scatter_box(seed + 7, m, cen[:2], box=(120.0, 120.0), z=(60.0, 180.0))
     n = len(pos)
-    src = W.t4010a1_records(pos, 1.0, 0.0)
+    src = W.t4010a1_records(pos, 1.0, 0.0) if st == 1 else W.sphere_records(pos, 1.0, 0.0)
     k = np.full(n, W.wavenumber(), np.float32)
     a = np.full(n, 1.15e-2, np.float32)
     amps = rng.uniform(0.5, 1.0, (K, n)).astype(np.float32)
@@ -30,13 +30,13 @@ def _problem(seed, n_tiles, m, K):
     return src, k, a, pts, amps, phases
 
 
-def _p64(src, k, a, pts, amps, phases):
-    g = O.build_g_f64(1, src, k, a, pts)  # unit amplitude, zero phase
+def _p64(src, k, a, pts, amps, phases, st=1):
+    g = O.build_g_f64(st, src, k, a, pts)  # unit amplitude, zero phase
     q = amps.astype(np.float64) * np.exp(1j * phases.astype(np.float64))
     return g @ q.T  # m x K
 
 
-def _run(afc, torch, prec, src, k, a, pts, amps, phases):
+def _run(afc, torch, prec, src, k, a, pts, amps, phases, st=1):
     n, m, K = len(k), len(pts), len(amps)
     dev = "cuda"
     d_src = torch.from_numpy(src.reshape(-1)).to(dev)
@@ -49,26 +49,26 @@ def _run(afc, torch, prec, src, k, a, pts, amps, phases):
     ws = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
     base = (ws.data_ptr() + 255) // 256 * 256
     out = torch.zeros(2 * m * K, dtype=torch.float32, device=dev)
-    st = torch.cuda.current_stream().cuda_stream
-    rc = afc.DLL.AFC_MultiPatternBuildG(1, prec, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
-                                        n, d_pts.data_ptr(), m, K, base, wsb, st)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = afc.DLL.AFC_MultiPatternBuildG(st, prec, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                        n, d_pts.data_ptr(), m, K, base, wsb, stream)
     assert rc == 0, afc.last_error()
     rc = afc.DLL.AFC_MultiPatternApply(prec, d_amps.data_ptr(), d_ph.data_ptr(), n, m, K,
-                                       out.data_ptr(), base, wsb, st)
+                                       out.data_ptr(), base, wsb, stream)
     assert rc == 0, afc.last_error()
-    assert afc.DLL.AFC_MultiPatternStatus(prec, n, m, K, base, st) == 0
+    assert afc.DLL.AFC_MultiPatternStatus(prec, n, m, K, base, stream) == 0
     torch.cuda.synchronize()
     return out.cpu().numpy().view(np.complex64).reshape(m, K)
 
 
-def _direct(afc, torch, src, k, a, pts, amps, phases):
+def _direct(afc, torch, src, k, a, pts, amps, phases, st=1):
     n, m, K = len(k), len(pts), len(amps)
     dev = "cuda"
     t = [torch.from_numpy(x.reshape(-1)).to(dev) for x in (src, k, a, pts, amps, phases)]
     wsb = 2 * afc.DLL.AFC_FieldWorkspaceBytes(n)
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     out = torch.zeros(2 * m * K, dtype=torch.float32, device=dev)
-    rc = afc.DLL.AFC_MultiPatternDirect(1, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), n,
+    rc = afc.DLL.AFC_MultiPatternDirect(st, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), n,
                                         t[3].data_ptr(), m, t[4].data_ptr(), t[5].data_ptr(), K,
                                         out.data_ptr(), ws.data_ptr(), wsb,
                                         torch.cuda.current_stream().cuda_stream)
@@ -80,6 +80,23 @@ def _direct(afc, torch, src, k, a, pts, amps, phases):
 def _errs(p, ref):
     return (float(np.max(np.abs(p - ref)) / np.max(np.abs(ref))),
             float(np.linalg.norm(p - ref) / np.linalg.norm(ref)))
+
+
+def test_multipattern_sphere_sources_vs_f64(gpu):
+    """The three forms on sphere sources (source type 0, D = 1), 249 sources x 1,000 points x
+    96 patterns, against float64."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    src, k, a, pts, amps, phases = _problem(77, (1, 1), 1000, 96, st=0)
+    ref = _p64(src, k, a, pts, amps, phases, st=0)
+    e_bf = _errs(_run(afc, torch, BF16X3, src, k, a, pts, amps, phases, st=0), ref)
+    e_h = _errs(_run(afc, torch, FP16, src, k, a, pts, amps, phases, st=0), ref)
+    e_d = _errs(_direct(afc, torch, src, k, a, pts, amps, phases, st=0), ref)
+    print(f"sphere: split-BF16 max {e_bf[0]:.2e} | FP16 max {e_h[0]:.2e} | FP32 direct max "
+          f"{e_d[0]:.2e}")
+    assert e_bf[0] <= 1e-4
+    assert e_d[0] <= 1e-4
+    assert e_h[0] <= 2e-3
 
 
 @pytest.mark.parametrize("K", [64, 128, 200])
