@@ -98,3 +98,24 @@ def test_nls_edge_cases(gpu):
     with pytest.raises(RuntimeError, match="too many foci"):
         afc.Optimizer.lm(s, big, np.ones(300, np.float32))
     np.testing.assert_array_equal(s.records(), before)
+
+
+@pytest.mark.parametrize("kind", sorted(KINDS))
+def test_nls_sphere_sources(gpu, kind):
+    """The three NLS solvers on sphere sources (source type 0, D = 1), 48 sources, 3 foci, with
+    the same comparison and bars as the T4010A1 cases."""
+    afc = gpu
+    rec9, k, a, foci, amps = _problem(700 + kind, 48, 3)
+    rec = W.sphere_records(rec9[:, :3], rec9[:, 6], rec9[:, 7])
+    s = afc.UniformSystem(300.0)
+    s.add_records(0, rec, k, a)
+    getattr(afc.Optimizer, KINDS[kind])(s, foci, amps)
+    got = s.records().copy()
+    ref = O.nls_f64(kind, 0, rec, k, a, foci, amps).reshape(-1, 6)
+    np.testing.assert_array_equal(got[:, 3], rec[:, 3])
+    p_gpu = np.abs(O.field_f64(0, got, k, a, foci))
+    p_ref = np.abs(O.field_f64(0, ref, k, a, foci))
+    err = float(np.max(np.abs(p_gpu - p_ref)) / np.max(p_ref))
+    print(f"{KINDS[kind]} sphere: rel {err:.2e}")
+    assert np.all(np.isfinite(got[:, 4]))
+    assert err <= {O.NLS_GRADIENT_DESCENT: 1e-4, O.NLS_LM: 1e-2, O.NLS_GAUSS_NEWTON: 5e-2}[kind]

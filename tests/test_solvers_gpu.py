@@ -142,3 +142,44 @@ def test_greedy_edge_cases(gpu):
     with pytest.raises(RuntimeError, match="phase_div"):
         afc.Optimizer.greedy(s, foci, amps, 0)
     np.testing.assert_array_equal(s.records(), before)
+
+
+@pytest.mark.parametrize("solver,tol", [("naive", 1e-5), ("gs", 1e-2)])
+def test_linear_synthesis_sphere_sources(gpu, solver, tol):
+    """Naive and GS on sphere sources (source type 0, D = 1), 996 sources, 16 foci, against the
+    float64 oracles with the T4010A1 cases' bars."""
+    afc = gpu
+    rng = np.random.default_rng(950 + len(solver))
+    w, foci, amps = W.gspat_request(rng, 16)
+    rec = W.sphere_records(w.sources[:, :3], w.sources[:, 6], w.sources[:, 7])
+    s = afc.UniformSystem(300.0)
+    s.add_records(0, rec, w.k, w.atten)
+    getattr(afc.Optimizer, solver)(s, foci, amps)
+    got = s.records().copy()
+    _, q_ref = {"naive": O.naive_f64, "gs": O.gs_f64}[solver](0, rec, w.k, w.atten, foci, amps)
+    q = got[:, 3].astype(np.float64) * np.exp(1j * got[:, 4].astype(np.float64))
+    e = np.max(np.abs(q - q_ref)) / np.max(np.abs(q_ref))
+    print(f"{solver} sphere: {e:.2e}")
+    assert e <= tol
+
+
+def test_greedy_sphere_sources(gpu):
+    """Greedy on sphere sources with the T4010A1 case's result bars."""
+    afc = gpu
+    rng = np.random.default_rng(960)
+    w, foci, amps = W.gspat_request(rng, 8)
+    rec = W.sphere_records(w.sources[:, :3], w.sources[:, 6], w.sources[:, 7])
+    s = afc.UniformSystem(300.0)
+    s.add_records(0, rec, w.k, w.atten)
+    afc.Optimizer.greedy(s, foci, amps, 16)
+    got = s.records().copy()
+    ref = O.greedy_f32(0, rec, w.k, w.atten, foci, amps, 16).reshape(-1, 6)
+    np.testing.assert_array_equal(got[:, 3], rec[:, 3])
+    same = float(np.mean(got[:, 4] == ref[:, 4]))
+    p_gpu = np.abs(O.field_f64(0, got, w.k, w.atten, foci))
+    p_ref = np.abs(O.field_f64(0, ref, w.k, w.atten, foci))
+    obj_gpu = float(np.sum(np.abs(amps - p_gpu)))
+    obj_ref = float(np.sum(np.abs(amps - p_ref)))
+    print(f"greedy sphere: identical choices {same:.3f}, objective {obj_gpu:.4e} vs {obj_ref:.4e}")
+    assert same >= 0.3
+    assert obj_gpu <= 1.1 * obj_ref + 1e-2 * float(np.sum(amps))
