@@ -518,3 +518,43 @@ def test_rows_tiling(gpu, dim, axes, counts, tilted):
         len(pts), 40000, replace=False)
     ref = O.field_f32(1, rec, k, a, pts[sel], O.FIELD_COMPLEX)
     assert rel_err(out[sel], ref) <= TOL
+
+
+def test_concurrent_calculators_match_serial(gpu):
+    """Four Python threads, each with its own calculator and field buffer, calculate at the same
+    time (ctypes releases the GIL around AFC_Calculate), five times each, on scatter and grid
+    areas of one system: every result equals the serial one bit for bit (each calculator has
+    its own stream and buffers; the kernels are deterministic)."""
+    import threading
+
+    afc = gpu
+    rng = np.random.default_rng(21)
+    rec, k, a = random_sources(rng, 1, 300)
+    s = make_system(afc, 1, rec, k, a)
+    pts = random_points(rng, 5000)
+    areas = [scatter(afc, pts),
+             afc.grid_from_spec(W.GridSpec(2, [(-30.0, 30.0), (-30.0, 30.0), (120.0, 120.0)], 0.5,
+                                           (1, 2, 3)))]
+    serial = [np.array(afc.GpuCalculator().calculate(s, ar, afc.ComplexPressureFieldBuffer()))
+              for ar in areas]
+    results, errors = [], []
+
+    def work(t):
+        try:
+            calc = afc.GpuCalculator()
+            f = afc.ComplexPressureFieldBuffer()
+            for it in range(5):
+                i = (t + it) % 2
+                results.append((i, np.array(calc.calculate(s, areas[i], f))))
+        except Exception as e:  # reported after the join
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    assert len(results) == 20
+    for i, r in results:
+        np.testing.assert_array_equal(r, serial[i])
