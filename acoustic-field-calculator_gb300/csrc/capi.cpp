@@ -311,6 +311,19 @@ void* make_grid(int dim, const float first[2], const float second[2], const floa
     return g;
 }
 
+// Points of a grid with per-axis counts c[0..2], false when the product does not fit in 62 bits
+// (counts that large come only from a zero-like resolution or a wrapped count, and would
+// otherwise be computed as a wrapped, meaningless size).
+bool grid_points_checked(const uint64_t c[3], uint64_t* out) {
+    unsigned __int128 p = 1;
+    for (int k = 0; k < 3; ++k) {
+        p *= c[k];
+        if (p > (static_cast<unsigned __int128>(1) << 62)) return false;
+    }
+    *out = static_cast<uint64_t>(p);
+    return true;
+}
+
 GridDev grid_dev(const Grid& g) {
     GridDev d;
     for (int k = 0; k < 3; ++k) {
@@ -612,6 +625,20 @@ uint64_t AFC_Calculate(void* calc_handle, void* system_handle, void* obs_handle,
         if (g && g->dim != obs_type + 1) {
             set_error("area type %d does not match the %dD grid handle", obs_type, g->dim);
             g = nullptr;
+        }
+        if (g) {
+            const GridDev d = grid_dev(*g);
+            const uint64_t c[3] = {static_cast<uint64_t>(d.count[0]),
+                                   static_cast<uint64_t>(d.count[1]),
+                                   static_cast<uint64_t>(d.count[2])};
+            uint64_t total = 0;
+            if (!grid_points_checked(c, &total)) {
+                set_error("grid has too many points (%llu x %llu x %llu)",
+                          static_cast<unsigned long long>(c[0]),
+                          static_cast<unsigned long long>(c[1]),
+                          static_cast<unsigned long long>(c[2]));
+                g = nullptr;
+            }
         }
         area = g;
     } else {
@@ -990,7 +1017,12 @@ int32_t AFC_FieldGridDevice(int32_t st, int32_t ft, int32_t sum, const float* d_
         ps.grid.origin[k] = grid->origin[k];
     }
     ps.grid.res = grid->res;
-    ps.m = ps.grid.count[0] * ps.grid.count[1] * ps.grid.count[2];
+    uint64_t total = 0;
+    if (!grid_points_checked(grid->count, &total)) {
+        set_error("grid has too many points");
+        return AFC_ERR_TOO_LARGE;
+    }
+    ps.m = static_cast<int64_t>(total);
     return device_field(st, ft, sum, d_sources, d_k, d_a, n, ps, d_out, ws, stream);
 }
 

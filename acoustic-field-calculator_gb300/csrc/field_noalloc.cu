@@ -84,7 +84,14 @@ extern "C" int32_t AFC_FieldGridDeviceNoAlloc(int32_t source_type, int32_t field
         ps.grid.origin[k] = grid->origin[k];
     }
     ps.grid.res = grid->res;
-    ps.m = ps.grid.count[0] * ps.grid.count[1] * ps.grid.count[2];
+    // the point count must not wrap (counts that large would otherwise give a meaningless size)
+    unsigned __int128 total = 1;
+    for (int k = 0; k < 3; ++k) {
+        total *= grid->count[k];
+        if (total > (static_cast<unsigned __int128>(1) << 62))
+            return fail(AFC_ERR_TOO_LARGE, "AFC_FieldGridDeviceNoAlloc: grid has too many points");
+    }
+    ps.m = static_cast<int64_t>(total);
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int dev = -1;

@@ -192,3 +192,17 @@ def test_workspace_bytes(afc_mod):
     assert afc_mod.DLL.AFC_FieldWorkspaceBytes(0) == 0
     assert afc_mod.DLL.AFC_FieldWorkspaceBytes(1) == 256
     assert afc_mod.DLL.AFC_FieldWorkspaceBytes(3984) >= 3984 * 48
+
+
+def test_grid_whose_point_count_would_wrap_is_rejected(afc_mod):
+    """Counts whose product does not fit in 62 bits (here 4,194,305 per axis) make AFC_Calculate
+    fail with an error before any device work, instead of computing a wrapped size.  (A zero
+    resolution keeps the reference's release-build behaviour: the count, inf as usize plus 1,
+    wraps to 0 and the field is empty.)"""
+    s = _system(afc_mod)
+    s.add_records(1, W.t4010a1_records(W.unit_array()[:5], 1.0, 0.0))
+    big = (afc_mod.GridAreaBuilder().x_range((0.0, 4194304.0)).y_range((0.0, 4194304.0))
+           .z_range((0.0, 4194304.0)).resolution(1.0).generate())
+    assert big.get_size() == (4194305, 4194305, 4194305)
+    with pytest.raises(RuntimeError, match="too many points"):
+        afc_mod.GpuCalculator().calculate(s, big, afc_mod.PressureFieldBuffer())
