@@ -313,7 +313,16 @@ extern "C" int32_t AFC_BatchCreate(int32_t source_type, const AfcFieldJob* jobs,
                 J.g.origin[k] = in.grid.origin[k];
             }
             J.g.res = in.grid.res;
-            J.m = J.g.count[0] * J.g.count[1] * J.g.count[2];
+            unsigned __int128 total = 1;  // checked after each factor: it must not wrap
+            for (int k = 0; k < 3; ++k) {
+                total *= in.grid.count[k];
+                if (total > (static_cast<unsigned __int128>(1) << 62)) {
+                    destroy(p);
+                    return fail(AFC_ERR_TOO_LARGE,
+                                "AFC_BatchCreate: a grid job has too many points");
+                }
+            }
+            J.m = static_cast<int64_t>(total);
         } else {
             J.g = GridDev{};
             J.g.count[0] = J.g.count[1] = J.g.count[2] = 1;

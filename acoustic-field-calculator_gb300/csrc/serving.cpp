@@ -411,6 +411,12 @@ bool valid_grid(const AfcGridDesc* g, GridDev* out) {
         out->origin[k] = g->origin[k];
     }
     out->res = g->res;
+    // the point count must not wrap (a request that large could never be admitted anyway)
+    unsigned __int128 total = 1;
+    for (int k = 0; k < 3; ++k) {
+        total *= g->count[k];
+        if (total > (static_cast<unsigned __int128>(1) << 62)) return false;
+    }
     return true;
 }
 
