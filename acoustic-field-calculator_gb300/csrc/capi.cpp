@@ -515,6 +515,10 @@ int32_t check_field_args(int32_t st, int32_t ft, int32_t sum, uint64_t n, const 
         set_error("invalid source/field/sum tag (%d, %d, %d)", st, ft, sum);
         return AFC_ERR_INVALID;
     }
+    if (n >= (1ull << 40)) {
+        set_error("too many sources (at most 2^40 per call)");
+        return AFC_ERR_TOO_LARGE;
+    }
     if (n > 0 && (!d_sources || !d_k || !d_a)) {
         set_error("source pointers are NULL");
         return AFC_ERR_INVALID;
@@ -988,6 +992,7 @@ int32_t AFC_GridDescFromArea(void* grid_handle, int32_t dimension, AfcGridDesc* 
 }
 
 size_t AFC_FieldWorkspaceBytes(uint64_t n_sources) {
+    if (n_sources >= (1ull << 40)) return 0;  // beyond what the field calls accept
     const size_t b = static_cast<size_t>(n_sources) * sizeof(PackedSource);
     return (b + 255) & ~static_cast<size_t>(255);
 }

@@ -469,6 +469,22 @@ struct Layout {
     size_t packed, a_hi, a_lo, b_hi, b_lo, row_inv, row_scale, c_pad, err, total;
 };
 
+// Sizes the contraction accepts: n and m below 2^31 (m a launch's row tiles), K within one
+// launch's column tiles, and a workspace whose size, recomputed in 128 bits, stays below 2^62
+// (so that no byte count wraps and a workspace sized by AFC_MultiPatternWorkspaceBytes always
+// covers what the kernels touch).
+bool sizes_ok(uint64_t n, uint64_t m, uint64_t K) {
+    if (n >= (1ull << 31) || m >= (1ull << 31) - BM || K >= (1ull << 26)) return false;
+    using u128 = unsigned __int128;
+    const u128 kpad = (2 * static_cast<u128>(n) + BK - 1) / BK * BK;
+    const u128 npad = (2 * static_cast<u128>(K) + BN - 1) / BN * BN;
+    if (npad / BN > 65535) return false;
+    const u128 total = 48 * static_cast<u128>(n) + 4 * static_cast<u128>(m) * kpad +
+                       4 * npad * kpad + 8 * static_cast<u128>(m) + 4 * static_cast<u128>(m) * npad +
+                       8 * 256;
+    return total < (static_cast<u128>(1) << 62);
+}
+
 Layout layout(int64_t n, int64_t m, int64_t K, int precision) {
     Layout L{};
     L.kpad = ((2 * n + BK - 1) / BK) * BK;
@@ -513,6 +529,7 @@ using namespace afc::mp;
 extern "C" size_t AFC_MultiPatternWorkspaceBytes(uint64_t n, uint64_t m, uint64_t patterns,
                                                  int32_t precision) {
     if (precision != AFC_PRECISION_BF16X3 && precision != AFC_PRECISION_FP16) return 0;
+    if (!sizes_ok(n, m, patterns)) return 0;
     return layout(static_cast<int64_t>(n), static_cast<int64_t>(m), static_cast<int64_t>(patterns),
                   precision)
         .total;
@@ -527,6 +544,10 @@ extern "C" int32_t AFC_MultiPatternBuildG(int32_t source_type, int32_t precision
         (source_type != SRC_SPHERE && source_type != SRC_T4010A1)) {
         set_error_message("AFC_MultiPatternBuildG: invalid precision or source type");
         return AFC_ERR_INVALID;
+    }
+    if (!sizes_ok(n, m, patterns)) {
+        set_error_message("AFC_MultiPatternBuildG: problem too large");
+        return AFC_ERR_TOO_LARGE;
     }
     const Layout L = layout(static_cast<int64_t>(n), static_cast<int64_t>(m),
                             static_cast<int64_t>(patterns), precision);
@@ -584,6 +605,10 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
     if (precision != AFC_PRECISION_BF16X3 && precision != AFC_PRECISION_FP16) {
         set_error_message("AFC_MultiPatternApply: invalid precision");
         return AFC_ERR_INVALID;
+    }
+    if (!sizes_ok(n, m, patterns)) {
+        set_error_message("AFC_MultiPatternApply: problem too large");
+        return AFC_ERR_TOO_LARGE;
     }
     const int64_t nn = static_cast<int64_t>(n), mm = static_cast<int64_t>(m),
                   K = static_cast<int64_t>(patterns);
@@ -719,6 +744,11 @@ extern "C" int32_t AFC_MultiPatternDirect(int32_t source_type, const float* d_so
                                           const float* d_amps, const float* d_phases,
                                           uint64_t patterns, float* d_out, void* d_ws,
                                           size_t ws_bytes, void* stream) {
+    if (n >= (1ull << 40) || m >= (1ull << 62) / 8 || patterns >= (1ull << 62) / 8 ||
+        (m && patterns > ((1ull << 62) / 8) / m)) {
+        set_error_message("AFC_MultiPatternDirect: problem too large");
+        return AFC_ERR_TOO_LARGE;
+    }
     const size_t half = AFC_FieldWorkspaceBytes(n);
     if ((source_type != SRC_SPHERE && source_type != SRC_T4010A1) || !d_out ||
         (n && (!d_sources || !d_wavenums || !d_attens || !d_amps || !d_phases || !d_ws ||

@@ -50,7 +50,8 @@ typedef struct AfcGridDesc {
 /* Describe a grid area handle (dimension 1, 2 or 3) for the device calls. */
 int32_t AFC_GridDescFromArea(void *grid_handle, int32_t dimension, AfcGridDesc *out);
 
-/* Bytes of device workspace the field calls need for n sources (16-byte aligned buffer). */
+/* Bytes of device workspace the field calls need for n sources (16-byte aligned buffer); 0 for
+ * n >= 2^40, which the field calls reject with AFC_ERR_TOO_LARGE. */
 size_t AFC_FieldWorkspaceBytes(uint64_t n_sources);
 
 /* Field of n sources on a grid.  d_out receives count[0]*count[1]*count[2] floats (pressure,
@@ -79,6 +80,9 @@ int32_t AFC_FieldScatterDevice(int32_t source_type, int32_t field_type, int32_t 
  * hi*hi + hi*lo + lo*hi accumulated in FP32; AFC_PRECISION_FP16: one FP16 product with each
  * row of G scaled by a power of two. */
 enum { AFC_PRECISION_BF16X3 = 1, AFC_PRECISION_FP16 = 2 };
+/* Workspace bytes for BuildG / Apply; 0 for an unknown precision or a problem beyond the limits
+ * (n, m < 2^31, patterns < 2^26, workspace < 2^62 bytes), which BuildG and Apply reject with
+ * AFC_ERR_TOO_LARGE. */
 size_t AFC_MultiPatternWorkspaceBytes(uint64_t n, uint64_t m, uint64_t patterns,
                                       int32_t precision);
 int32_t AFC_MultiPatternBuildG(int32_t source_type, int32_t precision, const float *d_sources,

@@ -206,3 +206,14 @@ def test_grid_whose_point_count_would_wrap_is_rejected(afc_mod):
     assert big.get_size() == (4194305, 4194305, 4194305)
     with pytest.raises(RuntimeError, match="too many points"):
         afc_mod.GpuCalculator().calculate(s, big, afc_mod.PressureFieldBuffer())
+
+
+def test_workspace_sizes_beyond_the_limits_are_zero(afc_mod):
+    """Sizes whose byte counts could wrap report a zero workspace (and the calls taking them
+    reject the problem) instead of a wrapped, too small size."""
+    dll = afc_mod.DLL
+    assert dll.AFC_FieldWorkspaceBytes(1 << 40) == 0
+    assert dll.AFC_MultiPatternWorkspaceBytes(1 << 31, 1000, 8, 1) == 0
+    assert dll.AFC_MultiPatternWorkspaceBytes(3984, 1 << 31, 8, 1) == 0
+    assert dll.AFC_MultiPatternWorkspaceBytes(1 << 30, 1 << 30, 8, 1) == 0
+    assert dll.AFC_MultiPatternWorkspaceBytes(3984, 262144, 1024, 1) > 8_000_000_000
