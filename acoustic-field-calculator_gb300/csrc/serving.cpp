@@ -399,6 +399,10 @@ class Engine {
     }
 };
 
+// Points of one request at most: 2^40 points need terabytes, far beyond any HBM budget, and keep
+// every byte count of the request far from wrapping.
+constexpr int64_t kMaxRequestPoints = 1LL << 40;
+
 bool valid_grid(const AfcGridDesc* g, GridDev* out) {
     if (!g) return false;
     bool seen[3] = {false, false, false};
@@ -539,6 +543,10 @@ extern "C" int64_t AFC_ServeSubmitField(void* engine, int32_t geometry, const fl
         r.ps.m = static_cast<int64_t>(n_points);
     }
     const int64_t n = gn, m = r.ps.m;
+    if (m < 0 || m > kMaxRequestPoints) {  // byte counts must not wrap; no budget holds this
+        set_error_message("AFC_ServeSubmitField: too many points");
+        return AFC_ERR_TOO_LARGE;
+    }
     r.out_bytes = field_elem_bytes(field_type) * static_cast<size_t>(m);
     r.user_out = h_out;
     const size_t pts_bytes = is_grid ? 0 : 12 * static_cast<size_t>(m);
@@ -578,6 +586,10 @@ extern "C" int64_t AFC_ServeSubmitGspat(void* engine, int32_t geometry, const fl
     }
     r.ps.m = r.ps.grid.count[0] * r.ps.grid.count[1] * r.ps.grid.count[2];
     const int64_t n = gn, M = r.n_foci;
+    if (r.ps.m > kMaxRequestPoints) {  // byte counts below must not wrap
+        set_error_message("AFC_ServeSubmitGspat: slice has too many points");
+        return AFC_ERR_TOO_LARGE;
+    }
     r.out_bytes = 4 * static_cast<size_t>(r.ps.m);
     r.out2_bytes = 8 * static_cast<size_t>(n);
     r.user_out = h_slice_out;
