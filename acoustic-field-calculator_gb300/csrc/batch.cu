@@ -284,12 +284,20 @@ extern "C" int32_t AFC_BatchCreate(int32_t source_type, const AfcFieldJob* jobs,
     for (uint64_t i = 0; i < n_jobs; ++i) {
         const AfcFieldJob& in = jobs[i];
         JobDev& J = p->jobs[i];
+        if (in.n_sources >= (1ull << 40) || (!in.is_grid && in.n_points >= (1ull << 62))) {
+            destroy(p);
+            return fail(AFC_ERR_TOO_LARGE, "AFC_BatchCreate: a job has too many sources or points");
+        }
         J.raw = in.d_sources;
         J.k = in.d_wavenums;
         J.atten = in.d_attens;
         J.n = static_cast<int64_t>(in.n_sources);
         J.src_off = off;
         off += J.n;
+        if (off >= (1LL << 40)) {  // the packed-source arena holds 48 bytes per source
+            destroy(p);
+            return fail(AFC_ERR_TOO_LARGE, "AFC_BatchCreate: too many sources over all jobs");
+        }
         J.field = in.field_type;
         J.is_grid = in.is_grid;
         J.out = in.d_out;
