@@ -1041,6 +1041,10 @@ int32_t AFC_FieldScatterDevice(int32_t st, int32_t ft, int32_t sum, const float*
         set_error("points pointer is NULL");
         return AFC_ERR_INVALID;
     }
+    if (m >= (1ull << 62)) {
+        set_error("too many points");
+        return AFC_ERR_TOO_LARGE;
+    }
     PointSet ps{};
     ps.is_grid = false;
     ps.pts = d_points;
