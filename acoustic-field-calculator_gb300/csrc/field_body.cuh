@@ -427,14 +427,64 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
     }
 }
 
-// Apply the field transform to a block's sums (block_accumulate) and store them.
+// Store the field of point p from its complex sum (vr, vi): the sum itself, its power
+// norm_sqr = re*re + im*im without contraction, or the pressure sqrt(norm_sqr)
+// (field_buffer/pressure_field.rs:35-37).
+__device__ __forceinline__ void store_field(void* __restrict__ out, int64_t p, int field, float vr,
+                                            float vi) {
+    if (field == FIELD_COMPLEX) {
+        reinterpret_cast<float2*>(out)[p] = make_float2(vr, vi);
+    } else {
+        const float ns = __fadd_rn(__fmul_rn(vr, vr), __fmul_rn(vi, vi));
+        reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
+    }
+}
+
+// Point p at (px, py, pz), already stored by this thread: if its field is NaN and sources sit
+// exactly on it, store the reference's field there.  At the reference's dist = 0
+// (uniform_medium.rs:113-119) such a source gives amp * D * exp(-0 alpha) / 0 with D = 1 (acos
+// of 0 / 0 is NaN: bin 0, t4010a1.rs:107-109), so from_polar gives components of +-inf, or NaN
+// where the amplitude is 0 or sin(phase) is 0.  No finite term changes such a sum (nor does the
+// Accurate tag's sorted sum), so the point's field is the sum of these terms alone.  The
+// kernels' pair math gives 0 * inf = NaN there instead.  A NaN without a coincident source (a
+// NaN coordinate or parameter) is left as stored.
+static __device__ __noinline__ void fix_coincident(const PackedSource* __restrict__ src,
+                                                   int64_t n, float px, float py, float pz,
+                                                   int64_t p, int field, void* __restrict__ out) {
+    const float v0 = field == FIELD_COMPLEX ? reinterpret_cast<const float2*>(out)[p].x
+                                            : reinterpret_cast<const float*>(out)[p];
+    const float v1 = field == FIELD_COMPLEX ? reinterpret_cast<const float2*>(out)[p].y : 0.f;
+    if (!isnan(v0) && !isnan(v1)) return;
+    float re = 0.f, im = 0.f;
+    bool hit = false;
+    for (int64_t j = 0; j < n; ++j) {
+        const float4 a = src[j].a;
+        if (ref_dist2_1(__fsub_rn(px, a.x), __fsub_rn(py, a.y), __fsub_rn(pz, a.z)) != 0.f)
+            continue;
+        const float4 b = src[j].b, c = src[j].c;
+        // amp * exp(-dist alpha) / dist and phase + k dist at dist = 0
+        const float w = __fdiv_rn(__fmul_rn(c.z, exp2f(__fmul_rn(0.f, b.w))), 0.f);
+        const float phi = __fadd_rn(c.w, __fmul_rn(a.w, 0.f));
+        re = __fadd_rn(re, __fmul_rn(w, cosf(phi)));
+        im = __fadd_rn(im, __fmul_rn(w, sinf(phi)));
+        hit = true;
+    }
+    if (hit) store_field(out, p, field, re, im);
+}
+
+// Apply the field transform to a block's sums (block_accumulate) and store them; points whose
+// sum is NaN are then passed to fix_coincident.  `grid`, `g` and `pts` give the points as block_accumulate
+// takes them.
 template <int SUM, int PAIRS>
 __device__ __forceinline__ void block_store(float2 (&RE)[PAIRS], float2 (&IM)[PAIRS],
                                             float2 (&CRE)[PAIRS], float2 (&CIM)[PAIRS],
-                                            int64_t first, int64_t m, int field,
-                                            void* __restrict__ out) {
+                                            const PackedSource* __restrict__ src, int64_t n,
+                                            bool grid, const GridDev& g,
+                                            const float* __restrict__ pts, int64_t first,
+                                            int64_t m, int field, void* __restrict__ out) {
     constexpr int kPPT = 2 * PAIRS;
     const int64_t base = first + threadIdx.x;
+    bool bad = false;
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         const int64_t p = base + static_cast<int64_t>(k) * kThreads;
@@ -445,12 +495,23 @@ __device__ __forceinline__ void block_store(float2 (&RE)[PAIRS], float2 (&IM)[PA
             vr = __fadd_rn(vr, lane_of(CRE[k >> 1], k & 1));
             vi = __fadd_rn(vi, lane_of(CIM[k >> 1], k & 1));
         }
-        if (field == FIELD_COMPLEX) {
-            reinterpret_cast<float2*>(out)[p] = make_float2(vr, vi);
-        } else {
-            // norm_sqr = re*re + im*im without contraction (pressure_field.rs:35-37)
-            const float ns = __fadd_rn(__fmul_rn(vr, vr), __fmul_rn(vi, vi));
-            reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
+        bad |= isnan(vr) || isnan(vi);
+        store_field(out, p, field, vr, vi);
+    }
+    if (bad) {
+#pragma unroll 1
+        for (int k = 0; k < kPPT; ++k) {
+            const int64_t p = base + static_cast<int64_t>(k) * kThreads;
+            if (p >= m) break;
+            float x, y, z;
+            if (grid) {
+                grid_point(g, p, x, y, z);
+            } else {
+                x = pts[3 * p];
+                y = pts[3 * p + 1];
+                z = pts[3 * p + 2];
+            }
+            fix_coincident(src, n, x, y, z, p, field, out);
         }
     }
 }
@@ -464,7 +525,7 @@ __device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* _
                                              int64_t first, int field, void* __restrict__ out) {
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
     block_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE, CIM);
-    block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
+    block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, grid, g, pts, first, m, field, out);
 }
 
 }  // namespace fb

@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                                      CIM);
     cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
     if (cg::this_cluster().block_rank() == 0)
-        block_store<SUM, PAIRS>(RE, IM, CRE, CIM, first, m, field, out);
+        block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, GRID, g, pts, first, m, field,
+                                out);
 }
 
 // Mid-size grids: the rows tiling with every tile's sources split over a cluster of S blocks,
@@ -162,7 +163,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                                     IM, CRE, CIM);
     cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
     if (cg::this_cluster().block_rank() == 0)
-        rows_store<SUM, PAIRS>(g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field, out);
+        rows_store<SUM, PAIRS>(src, n, g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM,
+                               field, out);
 }
 
 // Grids with more than one point along their second axis: tiles of TX = 1 << tx_log2 first-axis

@@ -339,9 +339,11 @@ __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const PackedSource
 
 }
 
-// Store the thread's sums of one tile of the rows tiling (field transform applied).
+// Store the thread's sums of one tile of the rows tiling (field transform applied); points
+// whose sum is NaN are then passed to fix_coincident with the n sources src.
 template <int SUM, int PAIRS>
-__device__ __forceinline__ void rows_store(const GridDev& g, int tx_log2, int64_t tiles0,
+__device__ __forceinline__ void rows_store(const PackedSource* __restrict__ src, int64_t n,
+                                           const GridDev& g, int tx_log2, int64_t tiles0,
                                            int64_t tiles1, int64_t tile, float2 (&RE)[PAIRS],
                                            float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
                                            float2 (&CIM)[PAIRS], int field,
@@ -355,6 +357,7 @@ __device__ __forceinline__ void rows_store(const GridDev& g, int tx_log2, int64_
     const int64_t i0 = (t0 << tx_log2) + tx;
     const int64_t i1b = (t1 * (kThreads >> tx_log2) + ty) * kPPT;
     if (i0 >= c0) return;
+    bool bad = false;
 #pragma unroll
     for (int k = 0; k < kPPT; ++k) {
         const int64_t i1 = i1b + k;
@@ -366,12 +369,18 @@ __device__ __forceinline__ void rows_store(const GridDev& g, int tx_log2, int64_
             vr = __fadd_rn(vr, lane_of(CRE[k >> 1], k & 1));
             vi = __fadd_rn(vi, lane_of(CIM[k >> 1], k & 1));
         }
-        if (field == FIELD_COMPLEX) {
-            reinterpret_cast<float2*>(out)[p] = make_float2(vr, vi);
-        } else {
-            // norm_sqr = re*re + im*im without contraction (pressure_field.rs:35-37)
-            const float ns = __fadd_rn(__fmul_rn(vr, vr), __fmul_rn(vi, vi));
-            reinterpret_cast<float*>(out)[p] = (field == FIELD_PRESSURE) ? __fsqrt_rn(ns) : ns;
+        bad |= isnan(vr) || isnan(vi);
+        store_field(out, p, field, vr, vi);
+    }
+    if (bad) {
+#pragma unroll 1
+        for (int k = 0; k < kPPT; ++k) {
+            const int64_t i1 = i1b + k;
+            if (i1 >= c1) break;
+            const int64_t p = (i2 * c1 + i1) * c0 + i0;
+            float x, y, z;
+            grid_point(g, p, x, y, z);
+            fix_coincident(src, n, x, y, z, p, field, out);
         }
     }
 }
@@ -385,7 +394,8 @@ __device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __r
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
     rows_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE, IM,
                                     CRE, CIM);
-    rows_store<SUM, PAIRS>(g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field, out);
+    rows_store<SUM, PAIRS>(src, n, g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field,
+                           out);
 }
 
 }  // namespace fb
