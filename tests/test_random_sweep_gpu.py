@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 FIELDS = {0: "PressureFieldBuffer", 1: "PowerFieldBuffer", 2: "ComplexPressureFieldBuffer"}
 CALCS = {0: "CpuCalculator", 1: "AccurateCalculator", 2: "GpuCalculator"}
-N_CASES = 48
+N_CASES = 200
 
 
 def _sources(rng, st, n, tilted, atten):
