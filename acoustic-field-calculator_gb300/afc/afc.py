@@ -4,8 +4,11 @@ names, argument meaning and tags are the same; see python/afc/afc.py:24-560 of t
 Differences:
   * every calculator computes on the GPU; a failed native call raises RuntimeError with the
     library's message instead of aborting the process;
-  * UniformSystem.add_wave_source_with_wavenum_atten and the Optimizer methods for GS-PAT / GS /
-    naive run on the GPU; the other optimizers raise RuntimeError (unsupported).
+  * every Optimizer method runs on the GPU except ifft, which raises RuntimeError
+    (unsupported: an image-file set-up step outside this library);
+  * additions marked NEW: explicit wavenumber / attenuation sources, a numpy view of the source
+    array, and opt-in source tracking (UniformSystem.track_sources / sources_changed) that lets
+    a calculator skip re-uploading sources that have not changed.
 """
 from __future__ import annotations
 
@@ -125,6 +128,20 @@ class UniformSystem:
         if self._source_type == 1:
             return ctypes.cast(ptr, POINTER(T4010A1 * size)).contents
         raise TypeError("Unknown source type")
+
+    def track_sources(self, enable: bool = True):
+        """NEW, opt-in: reuse the device copy of unchanged sources between calculations.
+        Writes through an array obtained earlier (get_wave_sources, records) must then be
+        announced with sources_changed(); changes made through this library are seen by
+        themselves."""
+        if _dll().AFC_UniformSystemTrackSources(self.handle, self._source_type,
+                                                1 if enable else 0) != 0:
+            _check()
+
+    def sources_changed(self):
+        """NEW: announce writes made through an earlier source array (see track_sources)."""
+        if _dll().AFC_UniformSystemSourcesChanged(self.handle, self._source_type) != 0:
+            _check()
 
     def records(self) -> np.ndarray:
         """NEW: a numpy view (n x 9 or n x 6 float32) of the system's source array."""

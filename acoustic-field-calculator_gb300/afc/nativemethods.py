@@ -129,6 +129,7 @@ REFERENCE_EXPORTS = [
 ]
 NEW_EXPORTS = [
     "AFC_AddSphereWaveSourceWithWavenumAtten", "AFC_AddT4010A1WithWavenumAtten",
+    "AFC_UniformSystemTrackSources", "AFC_UniformSystemSourcesChanged",
     "AFC_GetLastError", "AFC_ClearLastError",
     "AFC_GridDescFromArea", "AFC_FieldWorkspaceBytes", "AFC_FieldGridDevice",
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
@@ -241,6 +242,10 @@ def __init_new():
     AFC_DLL.AFC_AddSphereWaveSourceWithWavenumAtten.restype = None
     AFC_DLL.AFC_AddT4010A1WithWavenumAtten.argtypes = [c_void_p, T4010A1, c_float, c_float]
     AFC_DLL.AFC_AddT4010A1WithWavenumAtten.restype = None
+    AFC_DLL.AFC_UniformSystemTrackSources.argtypes = [c_void_p, c_int32, c_int32]
+    AFC_DLL.AFC_UniformSystemTrackSources.restype = c_int32
+    AFC_DLL.AFC_UniformSystemSourcesChanged.argtypes = [c_void_p, c_int32]
+    AFC_DLL.AFC_UniformSystemSourcesChanged.restype = c_int32
     AFC_DLL.AFC_GetLastError.argtypes = []
     AFC_DLL.AFC_GetLastError.restype = c_char_p
     AFC_DLL.AFC_ClearLastError.argtypes = []

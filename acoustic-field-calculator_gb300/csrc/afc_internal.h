@@ -72,8 +72,41 @@ RowsTiling rows_tiling(const GridDev& g, int64_t m, int pairs);
 cudaError_t launch_repack(const PackedSource* geom, const float* amps, const float* phases,
                           const float* amp_phase, int64_t n, PackedSource* out, cudaStream_t s);
 
-// Streaming multiprocessors of the current device (cached after the first query).
+// Streaming multiprocessors of the current device (cached per device after the first query).
 int num_sms();
+
+// Switches the calling thread's current device for the guard's lifetime and switches it back
+// when the guard goes out of scope, so that an entry point that has to launch on its stream's
+// (or handle's) device leaves the caller's current device as it found it.
+class DeviceGuard {
+   public:
+    DeviceGuard() = default;
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+    // Make `dev` current; no call when it already is.
+    cudaError_t set(int dev) {
+        int cur = -1;
+        cudaError_t e = cudaGetDevice(&cur);
+        if (e != cudaSuccess) return e;
+        if (cur == dev) return cudaSuccess;
+        if (!switched_) prev_ = cur;
+        e = cudaSetDevice(dev);
+        if (e == cudaSuccess) switched_ = true;
+        return e;
+    }
+    ~DeviceGuard() {
+        if (switched_) cudaSetDevice(prev_);
+    }
+
+   private:
+    int prev_ = -1;
+    bool switched_ = false;
+};
+
+// The device whose work `s` orders (the current device for the default stream, NULL).
+inline cudaError_t stream_device(cudaStream_t s, int* dev) {
+    return s ? cudaStreamGetDevice(s, dev) : cudaGetDevice(dev);
+}
 
 // Record `msg` as this thread's last error (read back by AFC_GetLastError).
 void set_error_message(const char* msg);

@@ -259,7 +259,8 @@ int solve_apo(int st, float* src, const float* k, const float* atten, int64_t n,
             return fail("cudaStreamCreate");
         }
     }
-    if ((e = cudaSetDevice(g_apo_device)) != cudaSuccess) return fail("cudaSetDevice");
+    DeviceGuard dg;  // the solver's device while it runs; the caller's again on return
+    if ((e = dg.set(g_apo_device)) != cudaSuccess) return fail("cudaSetDevice");
     cudaStream_t s = g_apo_stream;
     std::vector<float> raw(src, src + n * stride);
     for (int64_t j = 0; j < n; ++j) raw[j * stride + iphase] = 0.f;  // apo.rs:101-103

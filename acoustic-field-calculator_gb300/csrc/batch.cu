@@ -235,6 +235,8 @@ cudaError_t capture(Plan& p) {
 
 void destroy(Plan* p) {
     if (!p) return;
+    DeviceGuard dg;  // the plan's device while freeing; the caller's again on return
+    dg.set(p->device);
     if (p->cap) cudaStreamSynchronize(p->cap);
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->d_jobs) cudaFree(p->d_jobs);
@@ -274,10 +276,14 @@ extern "C" int32_t AFC_BatchCreate(int32_t source_type, const AfcFieldJob* jobs,
     Plan* p = new (std::nothrow) Plan;
     if (!p) return fail(AFC_ERR_INVALID, "AFC_BatchCreate: out of host memory");
     p->st = source_type;
-    cudaError_t e = cudaSuccess;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (s) cudaStreamGetDevice(s, &p->device); else cudaGetDevice(&p->device);
-    cudaSetDevice(p->device);
+    DeviceGuard dg;  // the plan's device while it is built; the caller's again on return
+    cudaError_t e = stream_device(s, &p->device);
+    if (e == cudaSuccess) e = dg.set(p->device);
+    if (e != cudaSuccess) {
+        destroy(p);
+        return fail(AFC_ERR_CUDA, "AFC_BatchCreate: stream device", e);
+    }
     p->n_jobs = static_cast<int64_t>(n_jobs);
     p->jobs.resize(n_jobs);
     int64_t off = 0;
@@ -420,6 +426,9 @@ extern "C" int32_t AFC_BatchRunOneByOne(void* plan, void* stream) {
     Plan* p = static_cast<Plan*>(plan);
     if (!p) return fail(AFC_ERR_INVALID, "AFC_BatchRunOneByOne: invalid plan");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DeviceGuard dg;  // the plan's device while launching; the caller's again on return
+    const cudaError_t de = dg.set(p->device);
+    if (de != cudaSuccess) return fail(AFC_ERR_CUDA, "AFC_BatchRunOneByOne: device", de);
     for (int64_t i = 0; i < p->n_jobs; ++i) {
         const JobDev& J = p->jobs[i];
         PackedSource* packed = p->d_arena + J.src_off;

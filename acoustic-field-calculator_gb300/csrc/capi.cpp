@@ -118,8 +118,14 @@ enum : uint32_t {
     MAGIC_DEAD = 0xDEADDEADu
 };
 
+// Systems get process-wide unique ids, so that a calculator's packed copy of one system's
+// sources is never taken for another system created later at the same address.
+std::atomic<uint64_t> g_system_uid{0};
+
 // UniformSystem (system/uniform_medium.rs:21-27): AoS sources in the ABI layout plus SoA
-// wavenumbers and attenuations.
+// wavenumbers and attenuations.  `generation` counts the changes the library knows of (its own
+// writes, handed-out pointers, announced edits); with `track` on, a calculator reuses its
+// device copy of the sources while (uid, generation) are those it packed.
 struct System {
     uint32_t magic = MAGIC_SYSTEM;
     int st;
@@ -128,6 +134,9 @@ struct System {
     std::vector<float> src;
     std::vector<float> k, atten;
     std::string info, src_info;
+    uint64_t uid = g_system_uid.fetch_add(1) + 1;
+    uint64_t generation = 0;
+    bool track = false;
     size_t count() const { return k.size(); }
 };
 
@@ -214,6 +223,9 @@ struct GpuCtx {
     uint64_t pts_version = ~0ull;
     DevBuf out;
     PinnedBuf staging;
+    // the system whose sources `packed` holds, at which generation (uid 0: none)
+    uint64_t packed_uid = 0, packed_gen = 0;
+    int64_t packed_n = -1;
     std::mutex mu;
 
     int32_t init() {
@@ -269,6 +281,14 @@ System* as_system(void* h, int st) {
         set_error("source type %d does not match the system (%d)", st, s->st);
         return nullptr;
     }
+    return s;
+}
+
+// A system about to have its sources written (by this library, or through a pointer it hands
+// out): its generation moves on, so no calculator reuses a copy packed before.
+System* as_system_for_write(void* h, int st) {
+    System* s = as_system(h, st);
+    if (s) ++s->generation;
     return s;
 }
 
@@ -346,7 +366,8 @@ int32_t gpu_calculate(Calculator* calc, System* sys, void* area, int area_type, 
     std::lock_guard<std::mutex> lock(g.mu);
     int32_t rc = g.init();
     if (rc != AFC_OK) return rc;
-    cudaError_t e = cudaSetDevice(g.device);
+    DeviceGuard dg;  // the calculator's device while it runs; the caller's again on return
+    cudaError_t e = dg.set(g.device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
 
     PointSet ps{};
@@ -388,7 +409,11 @@ int32_t gpu_calculate(Calculator* calc, System* sys, void* area, int area_type, 
     const int64_t n = static_cast<int64_t>(sys->count());
     const int stride = source_stride(sys->st);
     const size_t raw_floats = static_cast<size_t>(n) * (stride + 2);
-    if (n > 0) {
+    // opted-in systems whose sources have not changed since this calculator packed them
+    const bool reuse = sys->track && g.packed_uid == sys->uid && g.packed_gen == sys->generation &&
+                       g.packed_n == n;
+    g.packed_uid = 0;  // set again below once the packed copy is complete
+    if (n > 0 && !reuse) {
         if ((e = g.staging.ensure(raw_floats * sizeof(float))) != cudaSuccess)
             return cuda_fail(e, "cudaHostAlloc(staging)");
         float* st = static_cast<float*>(g.staging.p);
@@ -417,12 +442,17 @@ int32_t gpu_calculate(Calculator* calc, System* sys, void* area, int area_type, 
         return cuda_fail(e, "cudaMemcpyAsync(field)");
     if ((e = cudaStreamSynchronize(g.stream)) != cudaSuccess)
         return cuda_fail(e, "field calculation");
+    if (sys->track) {
+        g.packed_uid = sys->uid;
+        g.packed_gen = sys->generation;
+        g.packed_n = n;
+    }
     *out_len = static_cast<uint64_t>(ps.m);
     return AFC_OK;
 }
 
 void add_source(void* handle, int st, const float* rec, bool explicit_ka, float k, float a) {
-    System* s = as_system(handle, st);
+    System* s = as_system_for_write(handle, st);
     if (!s) return;
     const int stride = source_stride(st);
     const float freq = rec[stride - 1];
@@ -456,7 +486,7 @@ void run_solver(int kind, void* handle, const void* foci, const float* amps, uin
         set_error("unknown source type %d", st);
         return;
     }
-    System* s = as_system(handle, st);
+    System* s = as_system_for_write(handle, st);
     if (!s) return;
     std::vector<float> f, a;
     if (!unpack_foci(foci, amps, size, f, a)) return;
@@ -473,7 +503,7 @@ void run_nls(int kind, void* handle, const void* foci, const float* amps, uint64
         set_error("unknown source type %d", st);
         return;
     }
-    System* s = as_system(handle, st);
+    System* s = as_system_for_write(handle, st);
     if (!s) return;
     std::vector<float> f, a;
     if (!unpack_foci(foci, amps, size, f, a)) return;
@@ -490,7 +520,7 @@ void run_matrix(int kind, void* handle, const void* foci, const float* amps, uin
         set_error("unknown source type %d", st);
         return;
     }
-    System* s = as_system(handle, st);
+    System* s = as_system_for_write(handle, st);
     if (!s) return;
     std::vector<float> f, a;
     if (!unpack_foci(foci, amps, size, f, a)) return;
@@ -541,15 +571,12 @@ int32_t device_field(int32_t st, int32_t ft, int32_t sum, const float* d_sources
                      void* d_out, void* ws, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
-    if (s) {
-        // launch on the stream's device whatever device this thread last selected
-        int sdev = -1, cur = -1;
-        if ((e = cudaStreamGetDevice(s, &sdev)) != cudaSuccess)
-            return cuda_fail(e, "cudaStreamGetDevice");
-        if (cudaGetDevice(&cur) != cudaSuccess || cur != sdev) {
-            if ((e = cudaSetDevice(sdev)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-        }
-    }
+    // launch on the stream's device whatever device this thread last selected, and leave the
+    // caller's current device as it was
+    DeviceGuard dg;
+    int sdev = -1;
+    if ((e = stream_device(s, &sdev)) != cudaSuccess) return cuda_fail(e, "cudaStreamGetDevice");
+    if ((e = dg.set(sdev)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     if (n > 0) {
         e = launch_pack_sources(st, d_sources, d_k, d_a, static_cast<int64_t>(n),
                                 static_cast<PackedSource*>(ws), s);
@@ -745,10 +772,23 @@ void AFC_AddT4010A1WithWavenumAtten(void* handle, AfcT4010A1 source, float waven
 
 uint64_t AFC_GetWaveSources(void* handle, void** out, int32_t source_type) {
     if (out) *out = nullptr;
-    System* s = as_system(handle, source_type);
-    if (!s || !out) return 0;
+    if (!out) return 0;
+    // the caller may write through the pointer: the next calculation uploads the sources again
+    System* s = as_system_for_write(handle, source_type);
+    if (!s) return 0;
     *out = s->src.data();
     return s->count();
+}
+
+int32_t AFC_UniformSystemTrackSources(void* handle, int32_t source_type, int32_t enable) {
+    System* s = as_system_for_write(handle, source_type);
+    if (!s) return AFC_ERR_INVALID;
+    s->track = enable != 0;
+    return AFC_OK;
+}
+
+int32_t AFC_UniformSystemSourcesChanged(void* handle, int32_t source_type) {
+    return as_system_for_write(handle, source_type) ? AFC_OK : AFC_ERR_INVALID;
 }
 
 // ------------------------------------------------------------------ areas
@@ -859,7 +899,7 @@ void AFO_FocalPoint(void* handle, AfcVector3 point, int32_t source_type) {
         set_error("unknown source type %d", source_type);
         return;
     }
-    System* s = as_system(handle, source_type);
+    System* s = as_system_for_write(handle, source_type);
     if (!s) return;
     // focal_point.rs:28-39
     const int stride = source_stride(source_type);
@@ -899,7 +939,7 @@ void AFO_BesselBeam(void* handle, AfcVector3 point, AfcVector3 dir, float theta,
         set_error("unknown source type %d", source_type);
         return;
     }
-    System* s = as_system(handle, source_type);
+    System* s = as_system_for_write(handle, source_type);
     if (!s) return;
     const float vx = dir.y, vy = -dir.x, vz = 0.0f;
     const float theta_w = asinf(sqrtf(vx * vx + vy * vy + vz * vz));
@@ -941,7 +981,7 @@ void AFO_APO(void* handle, const void* foci, const float* amps, uint64_t size, f
         set_error("unknown source type %d", source_type);
         return;
     }
-    System* s = as_system(handle, source_type);
+    System* s = as_system_for_write(handle, source_type);
     if (!s) return;
     std::vector<float> f, a;
     if (!unpack_foci(foci, amps, size, f, a)) return;

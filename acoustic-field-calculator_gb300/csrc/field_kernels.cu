@@ -186,7 +186,10 @@ __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
     out[j] = pack_source(st, raw, k, atten, j);
 }
 
-int g_num_sms = 0;
+// SM count per device (0: not queried yet); devices past the cache are queried every time.
+constexpr int kSmCacheDevices = 64;
+constexpr int kFallbackSms = 148;
+std::atomic<int> g_num_sms[kSmCacheDevices] = {};
 
 // Cluster split of small launches: at most the portable cluster size, each block summing at
 // least kSplitMinSources sources.
@@ -338,15 +341,16 @@ RowsTiling rows_tiling(const GridDev& g, int64_t m, int pairs) {
 
 
 int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
-            g_num_sms = v;
-        else
-            return 148;
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return kFallbackSms;
+    if (dev < kSmCacheDevices) {
+        v = g_num_sms[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
     }
-    return g_num_sms;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+        return kFallbackSms;
+    if (dev < kSmCacheDevices) g_num_sms[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
 
 cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const float* atten,

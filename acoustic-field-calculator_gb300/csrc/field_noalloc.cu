@@ -95,12 +95,10 @@ extern "C" int32_t AFC_FieldGridDeviceNoAlloc(int32_t source_type, int32_t field
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int dev = -1;
-    cudaError_t e = s ? cudaStreamGetDevice(s, &dev) : cudaGetDevice(&dev);
+    cudaError_t e = stream_device(s, &dev);
     if (e != cudaSuccess) return fail(AFC_ERR_CUDA, cudaGetErrorString(e));
-    int cur = -1;
-    if (cudaGetDevice(&cur) != cudaSuccess || cur != dev) {
-        if ((e = cudaSetDevice(dev)) != cudaSuccess) return fail(AFC_ERR_CUDA, cudaGetErrorString(e));
-    }
+    DeviceGuard dg;  // the stream's device while launching; the caller's again on return
+    if ((e = dg.set(dev)) != cudaSuccess) return fail(AFC_ERR_CUDA, cudaGetErrorString(e));
     void* scratch = nullptr;
     if ((e = scratch_on(dev, &scratch)) != cudaSuccess)
         return fail(AFC_ERR_CUDA, cudaGetErrorString(e));

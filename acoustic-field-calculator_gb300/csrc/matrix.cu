@@ -280,7 +280,8 @@ int solve_matrix(int kind, int st, float* src, const float* k, const float* atte
             return fail("cudaStreamCreate");
         }
     }
-    if ((e = cudaSetDevice(g_mat_device)) != cudaSuccess) return fail("cudaSetDevice");
+    DeviceGuard dg;  // the solver's device while it runs; the caller's again on return
+    if ((e = dg.set(g_mat_device)) != cudaSuccess) return fail("cudaSetDevice");
     cudaStream_t s = g_mat_stream;
     // horn.rs:74-76, long.rs:51-53: phases zeroed, G from the zero-phase sources
     std::vector<float> raw(src, src + n * stride);

@@ -558,9 +558,17 @@ extern "C" int32_t AFC_MultiPatternBuildG(int32_t source_type, int32_t precision
     }
     if (n == 0 || m == 0) return AFC_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DeviceGuard dg;  // the stream's device while launching; the caller's again on return
+    int dev = 0;
+    cudaError_t e = stream_device(s, &dev);
+    if (e == cudaSuccess) e = dg.set(dev);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return AFC_ERR_CUDA;
+    }
     char* ws = static_cast<char*>(d_ws);
     auto* packed = reinterpret_cast<PackedSource*>(ws + L.packed);
-    cudaError_t e = launch_pack_sources(source_type, d_sources, d_wavenums, d_attens,
+    e = launch_pack_sources(source_type, d_sources, d_wavenums, d_attens,
                                         static_cast<int64_t>(n), packed, s);
     if (e != cudaSuccess) {
         set_error_message(cudaGetErrorString(e));
@@ -629,13 +637,19 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
         return AFC_ERR_CUDA;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DeviceGuard dg;  // the stream's device while launching; the caller's again on return
     int dev = 0;
-    if (s) cudaStreamGetDevice(s, &dev); else cudaGetDevice(&dev);
-    cudaSetDevice(dev);
+    if ((e = stream_device(s, &dev)) != cudaSuccess || (e = dg.set(dev)) != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return AFC_ERR_CUDA;
+    }
     char* ws = static_cast<char*>(d_ws);
     const bool split = precision == AFC_PRECISION_BF16X3;
     unsigned* err = reinterpret_cast<unsigned*>(ws + L.err);
-    cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+    if ((e = cudaMemsetAsync(err, 0, sizeof(unsigned), s)) != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return AFC_ERR_CUDA;
+    }
     // Q
     {
         const dim3 grid(static_cast<unsigned>((L.kpad / 2 + 255) / 256), static_cast<unsigned>(K));
@@ -649,11 +663,15 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
         count_launch();
         // B^T rows 2K .. npad-1 (padding) must be zero
         if (L.npad > 2 * K)
-            cudaMemsetAsync(ws + L.b_hi + static_cast<size_t>(2 * K) * L.kpad * 2, 0,
-                            static_cast<size_t>(L.npad - 2 * K) * L.kpad * 2, s);
-        if (split && L.npad > 2 * K)
-            cudaMemsetAsync(ws + L.b_lo + static_cast<size_t>(2 * K) * L.kpad * 2, 0,
-                            static_cast<size_t>(L.npad - 2 * K) * L.kpad * 2, s);
+            e = cudaMemsetAsync(ws + L.b_hi + static_cast<size_t>(2 * K) * L.kpad * 2, 0,
+                                static_cast<size_t>(L.npad - 2 * K) * L.kpad * 2, s);
+        if (e == cudaSuccess && split && L.npad > 2 * K)
+            e = cudaMemsetAsync(ws + L.b_lo + static_cast<size_t>(2 * K) * L.kpad * 2, 0,
+                                static_cast<size_t>(L.npad - 2 * K) * L.kpad * 2, s);
+        if (e != cudaSuccess) {
+            set_error_message(cudaGetErrorString(e));
+            return AFC_ERR_CUDA;
+        }
     }
     CUtensorMap ma0, ma1, mb0, mb1;
     if ((e = make_map(&ma0, ws + L.a_hi, split, mm, L.kpad, BM)) != cudaSuccess ||
@@ -711,6 +729,9 @@ extern "C" int32_t AFC_MultiPatternStatus(int32_t precision, uint64_t n, uint64_
                             static_cast<int64_t>(patterns), precision);
     unsigned h = 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DeviceGuard dg;
+    int dev = 0;
+    if (stream_device(s, &dev) != cudaSuccess || dg.set(dev) != cudaSuccess) return AFC_ERR_CUDA;
     if (cudaMemcpyAsync(&h, static_cast<char*>(d_ws) + L.err, sizeof(h), cudaMemcpyDeviceToHost, s) !=
             cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
@@ -759,12 +780,17 @@ extern "C" int32_t AFC_MultiPatternDirect(int32_t source_type, const float* d_so
     }
     if (m == 0 || patterns == 0) return AFC_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DeviceGuard dg;  // the stream's device while launching; the caller's again on return
     int dev = 0;
-    if (s) cudaStreamGetDevice(s, &dev); else cudaGetDevice(&dev);
-    cudaSetDevice(dev);
+    cudaError_t e = stream_device(s, &dev);
+    if (e == cudaSuccess) e = dg.set(dev);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return AFC_ERR_CUDA;
+    }
     auto* geom = static_cast<PackedSource*>(d_ws);
     auto* pat = reinterpret_cast<PackedSource*>(static_cast<char*>(d_ws) + half);
-    cudaError_t e = launch_pack_sources(source_type, d_sources, d_wavenums, d_attens,
+    e = launch_pack_sources(source_type, d_sources, d_wavenums, d_attens,
                                         static_cast<int64_t>(n), geom, s);
     PointSet ps{};
     ps.is_grid = false;

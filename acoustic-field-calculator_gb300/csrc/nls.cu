@@ -375,7 +375,8 @@ int solve_nls(int kind, int st, float* src, const float* k, const float* atten, 
             return fail("cudaStreamCreate");
         }
     }
-    if ((e = cudaSetDevice(g_nls.device)) != cudaSuccess) return fail("cudaSetDevice");
+    DeviceGuard dg;  // the solver's device while it runs; the caller's again on return
+    if ((e = dg.set(g_nls.device)) != cudaSuccess) return fail("cudaSetDevice");
     cudaStream_t s = g_nls.stream;
     const int64_t N = n + m;
     // phases are zeroed first (nls/*.rs: set_phase(0.)); G is built from the zero-phase sources

@@ -158,6 +158,8 @@ class Engine {
     ~Engine() { shutdown(); }
 
     void shutdown() {
+        DeviceGuard dg;  // the engine's device while tearing down; the caller's again after
+        dg.set(device);
         stop = true;
         cv_sched.notify_all();
         cv_host.notify_all();
@@ -478,7 +480,8 @@ extern "C" int32_t AFC_ServeAddGeometry(void* engine, int32_t source_type, const
     g.n = static_cast<int64_t>(n);
     const int stride = source_stride(source_type);
     const size_t raw_floats = static_cast<size_t>(n) * (stride + 2);
-    cudaError_t ce = cudaSetDevice(e->device);
+    DeviceGuard dg;  // the engine's device while uploading; the caller's again on return
+    cudaError_t ce = dg.set(e->device);
     if (ce == cudaSuccess) ce = cudaMalloc(&g.d_raw, sizeof(float) * (raw_floats ? raw_floats : 1));
     if (ce == cudaSuccess) ce = cudaMalloc(&g.d_packed, sizeof(PackedSource) * (n ? n : 1));
     if (ce == cudaSuccess && n) {

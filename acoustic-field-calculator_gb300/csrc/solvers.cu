@@ -455,7 +455,8 @@ int solve_multi_focus(int kind, int st, float* src, const float* k, const float*
             return fail("cudaStreamCreate");
         }
     }
-    if ((e = cudaSetDevice(c.device)) != cudaSuccess) return fail("cudaSetDevice");
+    DeviceGuard dg;  // the solver's device while it runs; the caller's again on return
+    if ((e = dg.set(c.device)) != cudaSuccess) return fail("cudaSetDevice");
     const int stride = source_stride(st);
     // input block: raw | k | atten | foci | amps [| candidate phasors | their arguments, from a
     // 16-byte boundary] ; output: 2n floats

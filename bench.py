@@ -16,6 +16,17 @@ Arms
              OpenMP over points) on a bounded z-slab of the same grid, on this host's cores;
              its `parity` checks the timed launches' field on that slab against the oracle's
              (max |p - p_ref| over the slab's peak |p_ref|, bar 1e-4).
+             After the headline and outside its timed region, the same line carries the other
+             configured workloads (skip them with --no-extras; single GPU only):
+               `single_focus_e2e`  the 249-source single focus through AFC_Calculate, us per
+                                   call by default and with opt-in source tracking, next to
+                                   the oracle's CPU time for the same call;
+               `multipattern`      1,024 patterns on 262,144 points x 3,984 sources: split-BF16
+                                   and FP16 tensor-core contractions and FP32 direct summation,
+                                   each with its error against float64 on 128 seeded rows;
+               `batch`             2,048 uneven jobs, graph replay vs one by one;
+               `serving`           Poisson streams at 1,000, 3,000 and 10,000 req/s: p50/p99,
+                                   achieved req/s and evals/s.
   reference  the reference's CPU calculator restated in C (the oracle: the Rust reference
              cannot be built here), all host threads, each step one bounded z-slab sample.
 
@@ -60,6 +71,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="grid: skip the other workloads that the default run measures after "
+                         "the headline (single focus end to end, multi-pattern, batch, "
+                         "serving)")
     ap.add_argument("--workload", default="grid",
                     choices=["grid", "multipattern", "batch", "serving"],
                     help="grid: the headline 256^3 field; multipattern: 1,024 patterns on "
@@ -396,6 +411,10 @@ def run_ours(args):
         slab = min(m, 64 * count * count)
         gpu_field = out[:2 * slab].cpu().numpy().view(np.complex64)
         line["cpu_baseline"] = cpu_baseline(w, gpu_field if count == 256 else None)
+    if world == 1 and count == 256 and not args.no_extras:
+        del out, ws, flush
+        torch.cuda.empty_cache()
+        line.update(secondary_workloads(afc, torch, local, args))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -403,27 +422,50 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ shared timing helper
+
+def event_times(torch, stream, fn, steps, warm):
+    """CUDA-event durations [s] of `steps` calls of fn on `stream` after `warm` untimed ones."""
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    return ts
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
 # ------------------------------------------------------------------ multi-pattern workload
 
 BF16X3, FP16 = 1, 2
 
 
-def run_multipattern(args):
-    """1,024 random patterns on the 3,984-source geometry at 262,144 scatter points:
-    P = G Q by split-BF16 and row-scaled FP16 tensor-core contractions and by FP32 direct
-    summation (one field launch per pattern).  value = split-BF16 source-point-pattern
-    evaluations per second of the contraction (G built beforehand, once per geometry)."""
-    import torch
-
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    import afc
+def multipattern_measure(afc, torch, local, m, K, steps, warmup, check_rows=128):
+    """1,024 random patterns (K) on the 3,984-source geometry at m scatter points: P = G Q by
+    the split-BF16 and row-scaled FP16 tensor-core contractions (G built once per geometry,
+    timed apart) and by FP32 direct summation (one field launch per pattern).  Each form's P is
+    compared on `check_rows` seeded rows (every pattern) with P computed in float64 from the
+    oracle's float64 G."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
 
     lib = afc.DLL
-    lib.AFC_SetDevice(local)
-    w, amps, phases = W.multi_pattern(m=args.mp_points, patterns=args.mp_patterns)
-    n, m, K = w.n, len(w.points), len(amps)
-    evals = n * m * K
+    w, amps, phases = W.multi_pattern(m=m, patterns=K)
+    n = w.n
     dev = torch.device("cuda", local)
     d_src = torch.from_numpy(w.sources.reshape(-1)).to(dev)
     d_k = torch.from_numpy(w.k).to(dev)
@@ -434,21 +476,20 @@ def run_multipattern(args):
     out = torch.empty(2 * m * K, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
+    rows = np.sort(np.random.default_rng(99).choice(m, min(check_rows, m), replace=False))
+    idx = torch.from_numpy(rows).to(dev)
+    # float64 reference on the sampled rows: G of unit amplitude and zero phase (the patterns
+    # carry the drive) times Q
+    unit = w.sources.copy()
+    unit[:, 6], unit[:, 7] = 1.0, 0.0
+    g64 = O.build_g_f64(1, unit, w.k, w.atten, w.points[rows])
+    p64 = g64 @ (amps.astype(np.float64) * np.exp(1j * phases.astype(np.float64))).T
 
-    def timed(fn, steps, warm):
-        for _ in range(warm):
-            fn()
-        torch.cuda.synchronize()
-        ts = []
-        for _ in range(steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1) * 1e-3)
-        return ts
+    def errs():
+        got = out.view(m, K, 2)[idx].cpu().numpy().view(np.complex64)[..., 0]
+        return {"max_abs_err_over_peak": float(np.max(np.abs(got - p64)) / np.max(np.abs(p64))),
+                "rel_l2_err": float(np.linalg.norm(got - p64) / np.linalg.norm(p64)),
+                "rows_checked": int(len(rows)), "against": "float64 (oracle G in float64)"}
 
     results = {}
     launches0 = lib.AFC_KernelLaunchCount()
@@ -468,11 +509,11 @@ def run_multipattern(args):
                                            out.data_ptr(), base, wsb, sh)
             assert rc == 0, afc.last_error()
 
-        tb = timed(build, 1, 1)
-        ta = timed(apply, args.steps, max(args.warmup, 1))
+        tb = event_times(torch, stream, build, 1, 1)
+        ta = event_times(torch, stream, apply, steps, max(warmup, 1))
         assert lib.AFC_MultiPatternStatus(prec, n, m, K, base, sh) == 0
-        results[name] = {"apply_s": statistics.median(ta), "build_g_s": tb[0],
-                         "workspace_gb": wsb / 1e9}
+        results[name] = {"apply_ms": statistics.median(ta) * 1e3, "build_g_ms": tb[0] * 1e3,
+                         "workspace_gb": wsb / 1e9, **errs()}
         del ws
     # FP32 direct summation: one field evaluation per pattern
     wsd = 2 * lib.AFC_FieldWorkspaceBytes(n)
@@ -484,55 +525,74 @@ def run_multipattern(args):
                                         K, out.data_ptr(), ws.data_ptr(), wsd, sh)
         assert rc == 0, afc.last_error()
 
-    td = timed(direct, 1, 1)
-    results["fp32_direct"] = {"apply_s": td[0]}
+    td = event_times(torch, stream, direct, 1, 1)
+    results["fp32_direct"] = {"apply_ms": td[0] * 1e3, **errs()}
     launches = lib.AFC_KernelLaunchCount() - launches0
-
-    bf = results["split_bf16"]["apply_s"]
+    del ws, out
+    evals = n * m * K
+    for v in results.values():
+        v["evals_per_s"] = evals / (v["apply_ms"] * 1e-3)
+    bf = results["split_bf16"]["apply_ms"] * 1e-3
     alg_flops = 8.0 * n * m * K  # 8 real flops per complex multiply-add
     kpad = (2 * n + 63) // 64 * 64
-    hw_flops = 3 * 2.0 * m * (2 * K) * kpad
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = peaks.get("bf16_tflops", 1900.0)
-    line = {"metric": "source-point-pattern evaluations/s (split-BF16 tensor-core contraction)",
-            "value": evals / bf, "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": bf * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (fp32 accumulate)",
-            "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "sources": n, "points": m, "patterns": K,
-                       "l2": "inputs (8.4 GB of G planes) larger than L2"},
-            "speedup_vs_fp32_direct": results["fp32_direct"]["apply_s"] / bf,
-            "results": {k: dict(v, evals_per_s=evals / v["apply_s"]) for k, v in results.items()},
-            "roofline": {"bound": "tensor", "achieved": alg_flops / bf / 1e12,
-                         "hardware_tflops": hw_flops / bf / 1e12, "peak": peak,
-                         "unit": "TFLOP/s", "frac": alg_flops / bf / 1e12 / peak,
-                         "frac_hardware": hw_flops / bf / 1e12 / peak,
-                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
-                         "traffic": None},
-            "gpu_launches": int(launches)}
-    print(json.dumps(line), flush=True)
+    hw_flops = 3 * 2.0 * m * (2 * K) * kpad  # hi.hi + hi.lo + lo.hi on the padded real GEMM
+    peak = measured_peaks().get("bf16_tflops")
+    peak_src = "MEASURED_PEAKS.json bf16_tflops (burst)"
+    if not peak:
+        peak, peak_src = 1900.0, "fallback 1.9 PFLOP/s (MEASURED_PEAKS.json absent)"
+    return {
+        "workload": w.name, "sources": n, "points": m, "patterns": K, "evals": evals,
+        "results": results,
+        "speedup_split_bf16_vs_fp32_direct": results["fp32_direct"]["apply_ms"] * 1e-3 / bf,
+        "speedup_fp16_vs_fp32_direct": results["fp32_direct"]["apply_ms"] /
+                                       results["fp16_row_scaled"]["apply_ms"],
+        "roofline": {"bound": "tensor", "achieved": alg_flops / bf / 1e12,
+                     "hardware_tflops": hw_flops / bf / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": alg_flops / bf / 1e12 / peak,
+                     "frac_hardware": hw_flops / bf / 1e12 / peak, "peak_source": peak_src,
+                     "note": "achieved = algorithmic flops (8 per complex MAC); hardware = "
+                             "the three BF16 products the split form issues"},
+        "gpu_launches": int(launches),
+    }
 
 
-# ------------------------------------------------------------------ batched uneven jobs
-
-def run_batch(args):
-    """2,048 independent field jobs (249/498/996/2,490 transducers, 1e3-1e6 points, half grid
-    slices, half scatter sets) as one persistent launch replayed from a CUDA graph, against
-    the same jobs launched one by one."""
+def run_multipattern(args):
+    """The multi-pattern workload alone: value = split-BF16 source-point-pattern evaluations
+    per second of the contraction."""
     import torch
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     import afc
+
+    afc.DLL.AFC_SetDevice(local)
+    r = multipattern_measure(afc, torch, local, args.mp_points, args.mp_patterns, args.steps,
+                             args.warmup)
+    bf = r["results"]["split_bf16"]
+    line = {"metric": "source-point-pattern evaluations/s (split-BF16 tensor-core contraction)",
+            "value": bf["evals_per_s"], "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": bf["apply_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (fp32 accumulate)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": r["workload"], "sources": r["sources"],
+                       "points": r["points"], "patterns": r["patterns"],
+                       "l2": "inputs (8.4 GB of G planes) larger than L2"},
+            "speedup_vs_fp32_direct": r["speedup_split_bf16_vs_fp32_direct"],
+            "results": r["results"], "roofline": r["roofline"],
+            "gpu_launches": r["gpu_launches"]}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ batched uneven jobs
+
+def batch_measure(afc, torch, n_jobs, steps, warmup, one_by_one_steps=3):
+    """n_jobs independent field jobs (249/498/996/2,490 transducers, 1e3-1e6 points, half grid
+    slices, half scatter sets) as one persistent launch replayed from a CUDA graph (autotuned
+    plan), against the same jobs launched one by one."""
     import batch_device as BD
 
     lib = afc.DLL
-    lib.AFC_SetDevice(local)
-    jobs = W.batch_jobs(n_jobs=args.batch_jobs)
+    jobs = W.batch_jobs(n_jobs=n_jobs)
     arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
@@ -541,52 +601,57 @@ def run_batch(args):
     create_s = time.perf_counter() - t0
     info = BD.describe(afc, plan)
 
-    def timed(fn, steps, warm):
-        for _ in range(warm):
-            fn()
-        torch.cuda.synchronize()
-        ts = []
-        for _ in range(steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1) * 1e-3)
-        return ts
-
     def run_graph():
         assert lib.AFC_BatchRun(plan, sh) == 0, afc.last_error()
 
     def run_each():
         assert lib.AFC_BatchRunOneByOne(plan, sh) == 0, afc.last_error()
 
-    launches0 = lib.AFC_KernelLaunchCount()
-    tb = timed(run_graph, args.steps, max(args.warmup, 1))
-    launches = (lib.AFC_KernelLaunchCount() - launches0) // (args.steps + max(args.warmup, 1))
-    te = timed(run_each, max(1, min(args.steps, 3)), 1)
-    lib.AFC_BatchFree(plan)
+    try:
+        launches0 = lib.AFC_KernelLaunchCount()
+        tb = event_times(torch, stream, run_graph, steps, max(warmup, 1))
+        launches = (lib.AFC_KernelLaunchCount() - launches0) // (steps + max(warmup, 1))
+        te = event_times(torch, stream, run_each, max(1, one_by_one_steps), 1)
+    finally:
+        lib.AFC_BatchFree(plan)
     evals = info["evals"]
     tbm, tem = statistics.median(tb), statistics.median(te)
+    return {"workload": f"batch_{len(jobs)}_uneven_jobs", "jobs": len(jobs),
+            "evals_per_step": evals, "points_per_step": int(sum(j.n_points for j in jobs)),
+            "autotuned": info, "plan_create_s": create_s,
+            "replay_ms": tbm * 1e3, "evals_per_s": evals / tbm,
+            "one_by_one_ms": tem * 1e3, "one_by_one_evals_per_s": evals / tem,
+            "one_by_one_launches_per_step": 2 * len(jobs),
+            "speedup_vs_one_by_one": tem / tbm, "gpu_launches_per_replay": int(launches)}
+
+
+def run_batch(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    import afc
+
+    afc.DLL.AFC_SetDevice(local)
+    r = batch_measure(afc, torch, args.batch_jobs, args.steps, args.warmup)
     line = {"metric": "source-point evaluations/s (2,048 uneven jobs, one persistent launch)",
-            "value": evals / tbm, "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tbm * 1e3, "higher_is_better": True,
+            "value": r["evals_per_s"], "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["replay_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": f"batch_{len(jobs)}_uneven_jobs", "jobs": len(jobs),
-                       "evals_per_step": evals,
-                       "points_per_step": int(sum(j.n_points for j in jobs)),
-                       "autotuned": info, "plan_create_s": create_s},
-            "one_by_one": {"value": evals / tem, "ms_per_step": tem * 1e3,
-                           "launches_per_step": 2 * len(jobs)},
-            "speedup_vs_one_by_one": tem / tbm,
-            "gpu_launches": int(launches)}
+            "config": {"workload": r["workload"], "jobs": r["jobs"],
+                       "evals_per_step": r["evals_per_step"],
+                       "points_per_step": r["points_per_step"], "autotuned": r["autotuned"],
+                       "plan_create_s": r["plan_create_s"]},
+            "one_by_one": {"value": r["one_by_one_evals_per_s"], "ms_per_step": r["one_by_one_ms"],
+                           "launches_per_step": r["one_by_one_launches_per_step"]},
+            "speedup_vs_one_by_one": r["speedup_vs_one_by_one"],
+            "gpu_launches": r["gpu_launches_per_replay"]}
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ serving
 
-def run_serving(args):
+def serving_measure(afc, lams, slots, warmup, max_requests=5000):
     """A seeded Poisson request stream through the serving engine (AFC_Serve*), swept over
     arrival rates: 70% field jobs drawn from a pool of the batched-job mix (the first 256
     jobs: 249-2,490 transducers, 1e3-1e6 points, grid slices and scatter sets), 30% GS-PAT
@@ -595,138 +660,215 @@ def run_serving(args):
     resident; each request uploads only its drive (or foci) and points, from host memory, and
     its result comes back to host memory.  Latency = submission to completion of the result's
     device-to-host copy, measured by the engine."""
+    import serving_client as SC
+
+    lib = afc.DLL
+    pool = W.batch_jobs(n_jobs=256)
+    eng = SC.Engine(afc, hbm_budget_bytes=2 << 30, pinned_bytes=2 << 30, max_inflight=slots)
+    try:
+        gid_of_n = {}
+        for jb in pool:
+            if jb.n not in gid_of_n:
+                gid_of_n[jb.n] = eng.add_geometry(1, jb.sources, jb.k, jb.atten)
+        gpos = W.tiled_array(2, 2)
+        gcen = W.array_center(gpos)
+        gsrc = W.t4010a1_records(gpos, 1.0, 0.0)
+        n_g = len(gpos)
+        gid_gspat = eng.add_geometry(1, gsrc, np.full(n_g, W.wavenumber(), np.float32),
+                                     np.zeros(n_g, np.float32))
+        # per pool job: (geometry, amps, phases, field type, grid desc or None, points, m, n)
+        payload = []
+        for jb in pool:
+            amps = np.ascontiguousarray(jb.sources[:, 6])
+            phases = np.ascontiguousarray(jb.sources[:, 7])
+            if jb.grid is not None:
+                desc = afc.grid_from_spec(jb.grid).grid_desc()
+                m = int(desc.count[0] * desc.count[1] * desc.count[2])
+                payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, desc, None, m, jb.n))
+            else:
+                pts = W.batch_job_points(jb)
+                payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, None, pts,
+                                jb.n_points, jb.n))
+        slice_evals = n_g * 201 * 201
+
+        def prepare(stream):
+            out = []
+            for r in stream:
+                if r.kind == "field":
+                    out.append(("field", r.arrival, payload[r.job]))
+                else:
+                    desc, _ = SC.slice_desc(afc, gcen, float(r.foci[:, 2].mean()), half=100.0,
+                                            res=1.0)
+                    out.append(("gspat", r.arrival, (r.foci, r.amps, desc)))
+            return out
+
+        def submit(item):
+            kind, _, p = item
+            if kind == "field":
+                gid, amps, phases, ft, desc, pts, m, n = p
+                rid, _ = eng.submit_field(gid, amps, phases, ft, grid=desc, points=pts)
+                return rid, n * m
+            foci, tamps, desc = p
+            rid, _, _ = eng.submit_gspat(gid_gspat, n_g, foci, tamps, desc)
+            return rid, slice_evals
+
+        def run_stream(items):
+            """Submit on the arrival schedule from this thread; a second thread waits."""
+            import queue as Q
+
+            q = Q.Queue()
+            lat, qwait = [], []
+            t_end = [0.0]
+
+            def waiter():
+                while True:
+                    got = q.get()
+                    if got is None:
+                        return
+                    rid, t_sub = got
+                    la, qw = eng.wait(rid)
+                    lat.append(la)
+                    qwait.append(qw)
+                    t_end[0] = max(t_end[0], t_sub + la)
+
+            th = threading.Thread(target=waiter)
+            th.start()
+            evals = 0
+            t0 = time.perf_counter()
+            for it in items:
+                while time.perf_counter() - t0 < it[1]:
+                    pass
+                t_sub = time.perf_counter()
+                rid, ev = submit(it)
+                evals += ev
+                q.put((rid, t_sub))
+            q.put(None)
+            th.join()
+            return np.asarray(lat), np.asarray(qwait), t_end[0] - t0, evals
+
+        warm = prepare(W.serving_stream(1000.0, max(warmup, 1) * 20, len(pool), seed=99))
+        run_stream(warm)
+        launches0 = lib.AFC_KernelLaunchCount()
+        st0 = eng.stats()
+        sweep = []
+        for i, lam in enumerate(lams):
+            n_req = int(min(max(lam * 2.0, 200), max_requests))
+            items = prepare(W.serving_stream(lam, n_req, len(pool), seed=4 + i))
+            lat, qw, span, evals = run_stream(items)
+            sweep.append({"offered_req_s": lam, "requests": n_req,
+                          "gspat_requests": sum(1 for it in items if it[0] == "gspat"),
+                          "achieved_req_s": n_req / span, "span_s": span,
+                          "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                          "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                          "queue_p50_ms": float(np.percentile(qw, 50) * 1e3),
+                          "queue_p99_ms": float(np.percentile(qw, 99) * 1e3),
+                          "evals_per_s": evals / span})
+        launches = lib.AFC_KernelLaunchCount() - launches0
+        st = eng.stats()
+    finally:
+        eng.close()
+    return {"workload": "serving_poisson_field70_gspat30", "pool_jobs": len(pool),
+            "gspat_sources": n_g, "gspat_foci": [2, 64], "gspat_iterations": 100,
+            "slice": [201, 201], "hbm_budget_bytes": st["hbm_budget_bytes"],
+            "max_inflight": slots, "sweep": sweep,
+            "engine": {"completed": st["completed"] - st0["completed"], "failed": st["failed"],
+                       "peak_inflight": st["peak_inflight"],
+                       "peak_hbm_bytes": st["peak_hbm_bytes"]},
+            "gpu_launches": int(launches)}
+
+
+def run_serving(args):
     import torch
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     import afc
-    import serving_client as SC
 
-    lib = afc.DLL
-    lib.AFC_SetDevice(local)
-    pool = W.batch_jobs(n_jobs=256)
-    eng = SC.Engine(afc, hbm_budget_bytes=2 << 30, pinned_bytes=2 << 30,
-                    max_inflight=args.serve_slots)
-    gid_of_n = {}
-    for jb in pool:
-        if jb.n not in gid_of_n:
-            gid_of_n[jb.n] = eng.add_geometry(1, jb.sources, jb.k, jb.atten)
-    gpos = W.tiled_array(2, 2)
-    gcen = W.array_center(gpos)
-    gsrc = W.t4010a1_records(gpos, 1.0, 0.0)
-    n_g = len(gpos)
-    gid_gspat = eng.add_geometry(1, gsrc, np.full(n_g, W.wavenumber(), np.float32),
-                                 np.zeros(n_g, np.float32))
-    # per pool job: (geometry, amps, phases, field type, grid desc or None, points or None, m)
-    payload = []
-    for jb in pool:
-        amps = np.ascontiguousarray(jb.sources[:, 6])
-        phases = np.ascontiguousarray(jb.sources[:, 7])
-        if jb.grid is not None:
-            desc = afc.grid_from_spec(jb.grid).grid_desc()
-            m = int(desc.count[0] * desc.count[1] * desc.count[2])
-            payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, desc, None, m, jb.n))
-        else:
-            pts = W.batch_job_points(jb)
-            payload.append((gid_of_n[jb.n], amps, phases, jb.field_type, None, pts,
-                            jb.n_points, jb.n))
-    slice_evals = n_g * 201 * 201
-
-    def prepare(stream):
-        out = []
-        for r in stream:
-            if r.kind == "field":
-                out.append(("field", r.arrival, payload[r.job]))
-            else:
-                desc, _ = SC.slice_desc(afc, gcen, float(r.foci[:, 2].mean()), half=100.0,
-                                        res=1.0)
-                out.append(("gspat", r.arrival, (r.foci, r.amps, desc)))
-        return out
-
-    def submit(item):
-        kind, _, p = item
-        if kind == "field":
-            gid, amps, phases, ft, desc, pts, m, n = p
-            rid, _ = eng.submit_field(gid, amps, phases, ft, grid=desc, points=pts)
-            return rid, n * m
-        foci, tamps, desc = p
-        rid, _, _ = eng.submit_gspat(gid_gspat, n_g, foci, tamps, desc)
-        return rid, slice_evals
-
-    def run_stream(items):
-        """Submit on the arrival schedule from this thread; a second thread waits."""
-        import queue as Q
-
-        q = Q.Queue()
-        lat, qwait = [], []
-        t_end = [0.0]
-
-        def waiter():
-            while True:
-                got = q.get()
-                if got is None:
-                    return
-                rid, t_sub = got
-                la, qw = eng.wait(rid)
-                lat.append(la)
-                qwait.append(qw)
-                t_end[0] = max(t_end[0], t_sub + la)
-
-        th = threading.Thread(target=waiter)
-        th.start()
-        evals = 0
-        t0 = time.perf_counter()
-        for it in items:
-            while time.perf_counter() - t0 < it[1]:
-                pass
-            t_sub = time.perf_counter()
-            rid, ev = submit(it)
-            evals += ev
-            q.put((rid, t_sub))
-        q.put(None)
-        th.join()
-        return np.asarray(lat), np.asarray(qwait), t_end[0] - t0, evals
-
+    afc.DLL.AFC_SetDevice(local)
     lams = [float(x) for x in args.lams.split(",")]
-    warm = prepare(W.serving_stream(1000.0, max(args.warmup, 1) * 20, len(pool), seed=99))
-    run_stream(warm)
-    launches0 = lib.AFC_KernelLaunchCount()
-    st0 = eng.stats()
-    sweep = []
-    for i, lam in enumerate(lams):
-        n_req = int(min(max(lam * 2.0, 200), 5000))
-        items = prepare(W.serving_stream(lam, n_req, len(pool), seed=4 + i))
-        lat, qw, span, evals = run_stream(items)
-        sweep.append({"offered_req_s": lam, "requests": n_req,
-                      "gspat_requests": sum(1 for it in items if it[0] == "gspat"),
-                      "achieved_req_s": n_req / span, "span_s": span,
-                      "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                      "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                      "queue_p50_ms": float(np.percentile(qw, 50) * 1e3),
-                      "queue_p99_ms": float(np.percentile(qw, 99) * 1e3),
-                      "field_evals_per_s": evals / span})
-    launches = lib.AFC_KernelLaunchCount() - launches0
-    st = eng.stats()
-    eng.close()
-    best = max(sweep, key=lambda s: s["achieved_req_s"])
+    r = serving_measure(afc, lams, args.serve_slots, args.warmup)
+    best = max(r["sweep"], key=lambda x: x["achieved_req_s"])
     line = {"metric": "requests/s (serving: Poisson stream, 70% field jobs / 30% GS-PAT)",
             "value": best["achieved_req_s"], "unit": "req/s", "n_gpus": 1,
             "steps": len(lams), "warmup": max(args.warmup, 1),
             "ms_per_step": best["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "serving_poisson_field70_gspat30", "pool_jobs": len(pool),
-                       "gspat_sources": n_g, "gspat_foci": [2, 64], "gspat_iterations": 100,
-                       "slice": [201, 201], "hbm_budget_bytes": st["hbm_budget_bytes"],
-                       "max_inflight": args.serve_slots},
-            "sweep": sweep,
-            "engine": {"completed": st["completed"] - st0["completed"], "failed": st["failed"],
-                       "peak_inflight": st["peak_inflight"],
-                       "peak_hbm_bytes": st["peak_hbm_bytes"]},
+            "config": {k: r[k] for k in ("workload", "pool_jobs", "gspat_sources", "gspat_foci",
+                                         "gspat_iterations", "slice", "hbm_budget_bytes",
+                                         "max_inflight")},
+            "sweep": r["sweep"], "engine": r["engine"],
             "e2e": {"value": best["achieved_req_s"], "unit": "req/s",
                     "note": "host buffers in and out; every request's copies are inside its "
                             "latency"},
-            "gpu_launches": int(launches)}
+            "gpu_launches": r["gpu_launches"]}
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ single focus, end to end
+
+def single_focus_e2e(afc, calls=200):
+    """The 249-transducer single focus (101 x 101 pressure slice at z = 150 mm) through the
+    reference-facing AFC_Calculate with host buffers, as the reference's example calls it:
+    wall-clock per call, by default (sources uploaded and packed on every call) and with the
+    opt-in source tracking (unchanged sources reused), next to the oracle's CPU time for the
+    same call on this host's cores.  The result is checked against the oracle."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    w = W.single_focus()
+    s = afc.UniformSystem(300.0)
+    s.add_records(1, w.sources, w.k, w.atten)
+    area = afc.grid_from_spec(w.grid)
+    calc = afc.GpuCalculator()
+    field = afc.PressureFieldBuffer()
+    out = {}
+    for mode, track in (("default", False), ("sources_tracked", True)):
+        s.track_sources(track)
+        for _ in range(20):
+            calc.calculate_raw(s, area, field)
+        t = []
+        for _ in range(calls):
+            t0 = time.perf_counter()
+            calc.calculate_raw(s, area, field)
+            t.append(time.perf_counter() - t0)
+        out[mode] = {"median_us": statistics.median(t) * 1e6,
+                     "p99_us": float(np.percentile(t, 99) * 1e6), "calls": calls}
+    s.track_sources(False)
+    got = calc.calculate(s, area, field)
+    lo, hi = w.grid.lo_hi()
+    pts = O.grid_points(2, lo, hi, w.grid.res, w.grid.axes)
+    O.field_f32(1, w.sources, w.k, w.atten, pts[:256], O.FIELD_PRESSURE)  # warm
+    tc = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ref = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_PRESSURE)
+        tc.append(time.perf_counter() - t0)
+    evals = w.n * len(pts)
+    cpu_us = statistics.median(tc) * 1e6
+    return {"workload": w.name, "sources": w.n, "points": len(pts), "evals": evals,
+            "api": "AFC_Calculate (reference C ABI), host buffers, one call per field",
+            **{f"{k}_us_per_call": v["median_us"] for k, v in out.items()},
+            "calls": out,
+            "evals_per_s": evals / (out["default"]["median_us"] * 1e-6),
+            "cpu_oracle_us_per_call": cpu_us, "cpu_oracle_threads": O.max_threads(),
+            "speedup_vs_cpu_oracle": cpu_us / out["default"]["median_us"],
+            "max_abs_err_over_peak": float(np.max(np.abs(got - ref)) / np.max(ref))}
+
+
+def secondary_workloads(afc, torch, local, args):
+    """The other configured workloads, measured after the headline and outside its timed
+    region, for the same JSON line."""
+    extras = {}
+    t0 = time.perf_counter()
+    extras["single_focus_e2e"] = single_focus_e2e(afc)
+    extras["multipattern"] = multipattern_measure(afc, torch, local, 262144, 1024,
+                                                  min(args.steps, 5), 2)
+    torch.cuda.empty_cache()
+    extras["batch"] = batch_measure(afc, torch, 2048, min(args.steps, 5), 1)
+    torch.cuda.empty_cache()
+    extras["serving"] = serving_measure(afc, [1000.0, 3000.0, 10000.0], args.serve_slots, 1)
+    extras["extras_wall_s"] = time.perf_counter() - t0
+    return extras
 
 
 def main():

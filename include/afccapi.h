@@ -94,6 +94,22 @@ void AFC_AddSphereWaveSourceWithWavenumAtten(void *handle, AfcSphereWaveSource s
                                             float wavenum, float atten);
 void AFC_AddT4010A1WithWavenumAtten(void *handle, AfcT4010A1 source, float wavenum, float atten);
 
+/* NEW, opt-in: skip the per-call source upload for callers that announce their edits.  The
+ * reference's AFC_GetWaveSources hands out the source array for writing in place, so by default
+ * every AFC_Calculate uploads and packs the system's sources again (capi/src/calculator.rs:
+ * 52-117 reads them on every call).  With tracking on (enable != 0), a calculator reuses the
+ * device copy it packed for this system in its previous calculation as long as the system's
+ * sources have not changed since: changes made by this library (AFC_Add*, AFO_*, or a new
+ * AFC_GetWaveSources pointer) are seen by themselves, while writes through a pointer obtained
+ * earlier must be announced with AFC_UniformSystemSourcesChanged before the next calculation,
+ * or that calculation uses the previous sources.  Turning tracking on or off also counts as
+ * a change.  Returns 0, or a negative AFC_ERR_* code (afc_gpu.h) for an invalid handle or
+ * tag. */
+int32_t AFC_UniformSystemTrackSources(void *handle, int32_t source_type, int32_t enable);
+/* NEW: announce that the system's sources were written through an AFC_GetWaveSources pointer
+ * (needed only while tracking is on; harmless otherwise). */
+int32_t AFC_UniformSystemSourcesChanged(void *handle, int32_t source_type);
+
 /* ---------------------------------------------------------------- observation areas */
 
 /* capi/src/observe_area.rs:20-27 */

@@ -217,3 +217,23 @@ def test_workspace_sizes_beyond_the_limits_are_zero(afc_mod):
     assert dll.AFC_MultiPatternWorkspaceBytes(3984, 1 << 31, 8, 1) == 0
     assert dll.AFC_MultiPatternWorkspaceBytes(1 << 30, 1 << 30, 8, 1) == 0
     assert dll.AFC_MultiPatternWorkspaceBytes(3984, 262144, 1024, 1) > 8_000_000_000
+
+
+def test_source_tracking_flags_check_their_handle(afc_mod):
+    """The opt-in source-tracking calls accept a system of the matching tag and reject anything
+    else with AFC_ERR_INVALID (-1), without touching the sources."""
+    s = _system(afc_mod)
+    s.add_records(1, W.t4010a1_records(W.unit_array()[:4], 1.0, 0.5))
+    before = s.records().copy()
+    dll = afc_mod.DLL
+    assert dll.AFC_UniformSystemTrackSources(s.handle, 1, 1) == 0
+    assert dll.AFC_UniformSystemSourcesChanged(s.handle, 1) == 0
+    assert dll.AFC_UniformSystemTrackSources(s.handle, 1, 0) == 0
+    assert dll.AFC_UniformSystemTrackSources(s.handle, 0, 1) == -1  # wrong source tag
+    assert "source type" in afc_mod.last_error()
+    assert dll.AFC_UniformSystemSourcesChanged(None, 1) == -1
+    area = afc_mod.GridAreaBuilder().x_range((0, 1)).y_at(0).z_at(10).resolution(1).generate()
+    assert dll.AFC_UniformSystemSourcesChanged(area.handle, 1) == -1  # not a system
+    np.testing.assert_array_equal(s.records(), before)
+    s.track_sources(True)
+    s.sources_changed()

@@ -1,8 +1,8 @@
 """Many patterns on one geometry: P = G Q on the tensor cores (split BF16 and row-scaled FP16)
 and by FP32 direct summation, against P computed in float64 from the oracle's G.
 
-Bars (max |P - P64| / max |P64|): split BF16 <= 1e-4, FP32 direct <= 1e-4, FP16 <= 2e-3
-(11-bit inputs)."""
+Bars (max |P - P64| / max |P64|): split BF16 <= 1e-4, FP32 direct <= 1e-4, FP16 <= 1e-3
+(11-bit inputs; measured <= 3.9e-4)."""
 import ctypes
 
 import numpy as np
@@ -96,7 +96,7 @@ def test_multipattern_sphere_sources_vs_f64(gpu):
           f"{e_d[0]:.2e}")
     assert e_bf[0] <= 1e-4
     assert e_d[0] <= 1e-4
-    assert e_h[0] <= 2e-3
+    assert e_h[0] <= 1e-3
 
 
 @pytest.mark.parametrize("K", [64, 128, 200])
@@ -113,7 +113,7 @@ def test_multipattern_precisions_vs_f64(gpu, K):
           f"rel-L2 {e_h[1]:.2e} | FP32 direct max {e_d[0]:.2e} rel-L2 {e_d[1]:.2e}")
     assert e_bf[0] <= 1e-4
     assert e_d[0] <= 1e-4
-    assert e_h[0] <= 2e-3
+    assert e_h[0] <= 1e-3
 
 
 def test_multipattern_full_size_sampled_rows_vs_f64(gpu):
@@ -135,7 +135,7 @@ def test_multipattern_full_size_sampled_rows_vs_f64(gpu):
          for x in (w.sources, w.k, w.atten, w.points, amps, phases)]
     st = torch.cuda.current_stream().cuda_stream
     idx = torch.from_numpy(rows).to(dev)
-    for prec, bar in ((BF16X3, 1e-4), (FP16, 2e-3)):
+    for prec, bar in ((BF16X3, 1e-4), (FP16, 1e-3)):
         wsb = afc.DLL.AFC_MultiPatternWorkspaceBytes(n, m, K, prec)
         ws = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
         base = (ws.data_ptr() + 255) // 256 * 256

@@ -3,8 +3,8 @@ restatement of acoustic-field-optimizer/src/multiple_foci/linear_synthesis/{gs_p
 
 The solvers write amp and phase into the system in place.  Compared quantity: the complex
 drive q_j = amp_j exp(i phase_j); bar: max |q_gpu - q_f64| <= tol * max |q_f64| with tol
-1e-3 (GS-PAT, 100 nonlinear FP32 iterations), 1e-5 (naive, one product) and 1e-2 (GS), and
-the field the drive produces at the foci."""
+1e-4 (GS-PAT, 100 nonlinear FP32 iterations; measured <= 2.0e-5), 1e-5 (naive, one product)
+and 1e-3 (GS; measured 2.4e-4), and the field the drive produces at the foci."""
 import numpy as np
 import pytest
 
@@ -38,7 +38,7 @@ def test_gspat_matches_f64(gpu, m):
     p_ref = np.abs(O.field_f64(1, ref_src, w.k, w.atten, foci))
     ef = np.max(np.abs(p_gpu - p_ref)) / np.max(p_ref)
     print(f"GS-PAT m={m}: max |dq|/max|q| = {e:.2e}, focus amplitude err {ef:.2e}")
-    assert e <= 1e-3
+    assert e <= 1e-4
     assert ef <= 1e-3
     # positions, directions and frequencies are untouched
     np.testing.assert_array_equal(got[:, [0, 1, 2, 3, 4, 5, 8]], w.sources[:, [0, 1, 2, 3, 4, 5, 8]])
@@ -67,7 +67,7 @@ def test_gs_matches_f64(gpu):
     ref_src, q_ref = O.gs_f64(1, w.sources, w.k, w.atten, foci, amps)
     e = np.max(np.abs(_q(got) - q_ref)) / np.max(np.abs(q_ref))
     print(f"GS: {e:.2e}")
-    assert e <= 1e-2
+    assert e <= 1e-3
 
 
 def test_gspat_then_field(gpu):

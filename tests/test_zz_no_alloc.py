@@ -12,6 +12,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle as O
 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -47,6 +48,13 @@ def _no_alloc(afc, w, desc, out, d_src, d_k, d_a, stream):
                                               out.data_ptr(), stream)
 
 
+def _oracle_sample(w, rows):
+    """The oracle's field (the reference CPU calculator restated) at grid points `rows`."""
+    lo, hi = w.grid.lo_hi()
+    pts = O.grid_points(3, lo, hi, w.grid.res, w.grid.axes)[rows]
+    return O.field_f32(1, w.sources, w.k, w.atten, pts)
+
+
 def test_no_alloc_matches_workspace_entry_point_twice(gpu):
     torch = pytest.importorskip("torch")
     afc = gpu
@@ -55,6 +63,8 @@ def test_no_alloc_matches_workspace_entry_point_twice(gpu):
     for tiles, seed in (((4, 4), 11), ((2, 2), 12)):
         w, area, desc, m, d_src, d_k, d_a = _setup(afc, torch, tiles, seed, 48)
         ref = _with_workspace(afc, torch, w, desc, m, d_src, d_k, d_a, stream)
+        rows = np.sort(np.random.default_rng(seed).choice(m, 2000, replace=False))
+        want = _oracle_sample(w, rows)
         for _ in range(2):
             out = torch.full((2 * m,), float("nan"), dtype=torch.float32, device="cuda")
             rc = _no_alloc(afc, w, desc, out, d_src, d_k, d_a, stream)
@@ -64,6 +74,8 @@ def test_no_alloc_matches_workspace_entry_point_twice(gpu):
             b = ref.cpu().numpy().view(np.complex64)
             assert np.all(np.isfinite(a))
             assert np.max(np.abs(a - b)) <= TOL * np.max(np.abs(b))
+            # and against the oracle itself, so that a fault shared by both entry points shows
+            assert np.max(np.abs(a[rows] - want)) <= TOL * np.max(np.abs(want))
 
 
 def test_no_alloc_rejects_more_sources_than_its_scratch(gpu):
