@@ -485,8 +485,13 @@ def multipattern_measure(afc, torch, local, m, K, steps, warmup, check_rows=128)
     g64 = O.build_g_f64(1, unit, w.k, w.atten, w.points[rows])
     p64 = g64 @ (amps.astype(np.float64) * np.exp(1j * phases.astype(np.float64))).T
 
-    def errs():
-        got = out.view(m, K, 2)[idx].cpu().numpy().view(np.complex64)[..., 0]
+    def errs(pattern_major=False):
+        # the contractions store P point-major (m x K), the direct path pattern by pattern
+        if pattern_major:
+            got = out.view(K, m, 2)[:, idx].permute(1, 0, 2).contiguous()
+        else:
+            got = out.view(m, K, 2)[idx]
+        got = got.cpu().numpy().view(np.complex64)[..., 0]
         return {"max_abs_err_over_peak": float(np.max(np.abs(got - p64)) / np.max(np.abs(p64))),
                 "rel_l2_err": float(np.linalg.norm(got - p64) / np.linalg.norm(p64)),
                 "rows_checked": int(len(rows)), "against": "float64 (oracle G in float64)"}
@@ -526,7 +531,7 @@ def multipattern_measure(afc, torch, local, m, K, steps, warmup, check_rows=128)
         assert rc == 0, afc.last_error()
 
     td = event_times(torch, stream, direct, 1, 1)
-    results["fp32_direct"] = {"apply_ms": td[0] * 1e3, **errs()}
+    results["fp32_direct"] = {"apply_ms": td[0] * 1e3, **errs(pattern_major=True)}
     launches = lib.AFC_KernelLaunchCount() - launches0
     del ws, out
     evals = n * m * K

@@ -29,6 +29,7 @@
  *   focal law          acoustic-field-optimizer/src/focal_point.rs:27-40
  *   G build            acoustic-field-optimizer/src/multiple_foci/macros.rs:17-53
  *   GS-PAT             acoustic-field-optimizer/src/multiple_foci/linear_synthesis/gs_pat.rs:35-81
+ *                      (float64, and in f32 as the reference computes it)
  *   GS                 acoustic-field-optimizer/src/multiple_foci/linear_synthesis/gs.rs:33-78
  *   Naive              acoustic-field-optimizer/src/multiple_foci/linear_synthesis/naive.rs:29-51
  *
@@ -995,6 +996,101 @@ ORC_EXPORT void oracle_gspat_f64(int st, float *src, const float *k, const float
     free(p);
     free(gamma);
     free(q);
+}
+
+typedef struct {
+    float re, im;
+} cplxf;
+
+/* num-complex Complex<f32> arithmetic: (a re - b im, a im + b re) per product, hypotf modulus. */
+static inline cplxf cmulf(cplxf a, cplxf b) {
+    cplxf r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+    return r;
+}
+static inline cplxf caddf(cplxf a, cplxf b) {
+    cplxf r = {a.re + b.re, a.im + b.im};
+    return r;
+}
+
+/* gs_pat.rs:38-81 in f32, as the reference computes it: G from the f32 propagate (phases
+ * zeroed), den_j = sum_i |G_ij| (nalgebra row_sum, rows in order), B = (conj(G_ij) / (den_j
+ * den_j))^T, R = G B and every matrix-vector product as nalgebra's gemv without BLAS (columns
+ * accumulated in order: y = x_0 A_0, then y += x_c A_c), the 100 normalisations
+ * gamma / |gamma| * p0, the final gamma / (|gamma| |gamma|) * p0 * p0, and q = B p, whose
+ * modulus and argument (hypotf, atan2f) become each source's amp and phase.  Updates `src` in
+ * place; q_out (2n doubles) receives q. */
+ORC_EXPORT void oracle_gspat_f32(int st, float *src, const float *k, const float *atten,
+                                 int64_t n, const float *foci, const float *amps, int64_t m,
+                                 int repeat, double *q_out) {
+    const int stride = src_stride(st);
+    const int iamp = st == ORC_SRC_T4010A1 ? 6 : 3;
+    const int iphase = st == ORC_SRC_T4010A1 ? 7 : 4;
+    for (int64_t j = 0; j < n; ++j) src[stride * j + iphase] = 0.0f;
+    cplxf *G = (cplxf *)malloc(sizeof(cplxf) * (size_t)(m * n)); /* G[i*n + j] */
+    oracle_build_g_f32(st, src, k, atten, n, foci, m, (float *)G);
+    float *den = (float *)calloc((size_t)n, sizeof(float));
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = 0; i < m; ++i) den[j] += hypotf(G[i * n + j].re, G[i * n + j].im);
+    cplxf *B = (cplxf *)malloc(sizeof(cplxf) * (size_t)(m * n)); /* B[j*m + i], n x m */
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t j = 0; j < n; ++j) {
+            const float s = den[j] * den[j];
+            cplxf b = {G[i * n + j].re / s, -G[i * n + j].im / s};
+            B[j * m + i] = b;
+        }
+    /* R = G B (m x m): column c = sum_j B[j, c] G[:, j] */
+    cplxf *R = (cplxf *)malloc(sizeof(cplxf) * (size_t)(m * m)); /* R[i*m + c] */
+    for (int64_t c = 0; c < m; ++c)
+        for (int64_t i = 0; i < m; ++i) {
+            cplxf acc = cmulf(B[0 * m + c], G[i * n + 0]);
+            for (int64_t j = 1; j < n; ++j) acc = caddf(cmulf(B[j * m + c], G[i * n + j]), acc);
+            R[i * m + c] = acc;
+        }
+    cplxf *p = (cplxf *)malloc(sizeof(cplxf) * (size_t)m);
+    cplxf *gamma = (cplxf *)malloc(sizeof(cplxf) * (size_t)m);
+    for (int64_t i = 0; i < m; ++i) {
+        p[i].re = amps[i];
+        p[i].im = 0.0f;
+    }
+    for (int it = 0; it <= repeat; ++it) {
+        /* gamma = R p: gamma_i = sum_c p_c R[i, c] */
+        for (int64_t i = 0; i < m; ++i) {
+            cplxf acc = cmulf(p[0], R[i * m + 0]);
+            for (int64_t c = 1; c < m; ++c) acc = caddf(cmulf(p[c], R[i * m + c]), acc);
+            gamma[i] = acc;
+        }
+        if (it == repeat) break;
+        for (int64_t i = 0; i < m; ++i) {
+            const float a = hypotf(gamma[i].re, gamma[i].im);
+            const cplxf g = {gamma[i].re / a, gamma[i].im / a};
+            const cplxf p0 = {amps[i], 0.0f};
+            p[i] = cmulf(g, p0);
+        }
+    }
+    for (int64_t i = 0; i < m; ++i) {
+        const float a = hypotf(gamma[i].re, gamma[i].im);
+        const float s = a * a;
+        const cplxf g = {gamma[i].re / s, gamma[i].im / s};
+        const cplxf p0 = {amps[i], 0.0f};
+        p[i] = cmulf(cmulf(g, p0), p0);
+    }
+    /* q = B p: q_j = sum_i p_i B[j, i] */
+    for (int64_t j = 0; j < n; ++j) {
+        cplxf acc = cmulf(p[0], B[j * m + 0]);
+        for (int64_t i = 1; i < m; ++i) acc = caddf(cmulf(p[i], B[j * m + i]), acc);
+        src[stride * j + iamp] = hypotf(acc.re, acc.im);
+        src[stride * j + iphase] = atan2f(acc.im, acc.re);
+        if (q_out) {
+            q_out[2 * j] = acc.re;
+            q_out[2 * j + 1] = acc.im;
+        }
+    }
+    free(G);
+    free(den);
+    free(B);
+    free(R);
+    free(p);
+    free(gamma);
 }
 
 /* naive.rs:29-51 in double: q = G^H p. */

@@ -70,6 +70,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_build_g_f32.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, fp]
         L.oracle_build_g_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, c_int64, dp, c_int]
         L.oracle_gspat_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, c_int, dp]
+        L.oracle_gspat_f32.argtypes = L.oracle_gspat_f64.argtypes
         L.oracle_gs_f64.argtypes = L.oracle_gspat_f64.argtypes
         L.oracle_naive_f64.argtypes = [c_int, fp, fp, fp, c_int64, fp, fp, c_int64, dp]
         L.oracle_max_threads.restype = c_int
@@ -293,6 +294,11 @@ def _solver(fn_name, st, sources, k, atten, foci, amps, repeat=None):
 def gspat_f64(st, sources, k, atten, foci, amps, repeat=100):
     """GS-PAT in float64; returns (updated sources, complex q)."""
     return _solver("oracle_gspat_f64", st, sources, k, atten, foci, amps, repeat)
+
+
+def gspat_f32(st, sources, k, atten, foci, amps, repeat=100):
+    """GS-PAT in f32 with the reference's operation order; returns (updated sources, q)."""
+    return _solver("oracle_gspat_f32", st, sources, k, atten, foci, amps, repeat)
 
 
 def gs_f64(st, sources, k, atten, foci, amps, repeat=100):

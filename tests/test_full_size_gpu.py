@@ -16,7 +16,9 @@ results is compared with the oracle and a sample of GS-PAT drives with the float
 of gs_pat.rs.
 
 Bars: max |p - p_ref| <= 1e-4 * max |p_ref| on the sampled points (2e-4 for the power field,
-whose relative error doubles); GS-PAT drive max |q - q64| <= 1e-4 * max |q64|.
+whose relative error doubles), for field results and for the GS-PAT slices (the field of the
+served drive); GS-PAT drive max |q - q64| <= max(1e-4, 3 e32) * max |q64|, e32 the distance
+from float64 of the reference's own f32 arithmetic on the same request (see GSPAT_SPREAD).
 """
 import numpy as np
 import pytest
@@ -30,6 +32,11 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-4
 SAMPLE_POINTS = 400
+# GS-PAT's 100 normalised iterations converge to a fixed point that rounding moves on
+# ill-conditioned foci sets: the reference's own f32 arithmetic (the oracle's gspat_f32) lands
+# up to 1.6e-3 of the peak drive from float64 on requests of this stream, against a median of
+# 1.1e-5.  A served drive must lie within max(1e-4, GSPAT_SPREAD x that f32 distance) of float64.
+GSPAT_SPREAD = 3.0
 
 
 def _transform(ref_c, ft):
@@ -50,7 +57,7 @@ def _as_field(arr, ft):
 
 def _sample_jobs(jobs, rng):
     """Indices of a job sample: for every (source count, grid or scatter, field type) the
-    largest job and one other at random, and the 8 largest jobs overall."""
+    largest job and two others at random, and the 8 largest jobs overall."""
     pick = set()
     groups = {}
     for i, jb in enumerate(jobs):
@@ -58,8 +65,8 @@ def _sample_jobs(jobs, rng):
     for key, idx in groups.items():
         idx = sorted(idx, key=lambda i: -jobs[i].n_points)
         pick.add(idx[0])
-        if len(idx) > 1:
-            pick.add(int(rng.choice(idx[1:])))
+        rest = idx[1:]
+        pick.update(int(i) for i in rng.choice(rest, min(2, len(rest)), replace=False))
     pick.update(sorted(range(len(jobs)), key=lambda i: -jobs[i].n_points)[:8])
     return sorted(pick)
 
@@ -199,8 +206,11 @@ def test_serving_stream_at_load_same_alone_and_vs_oracle(gpu):
         slice_out, ap = mixed[i]
         q = ap[0::2].astype(np.float64) * np.exp(1j * ap[1::2].astype(np.float64))
         _, q64 = O.gspat_f64(1, gsrc, gk, ga, r.foci, r.amps)
+        _, q32 = O.gspat_f32(1, gsrc, gk, ga, r.foci, r.amps)
         e = float(np.max(np.abs(q - q64)) / np.max(np.abs(q64)))
-        assert e <= TOL, f"GS-PAT request {i} (M={len(r.foci)}): drive {e:.3e}"
+        e32 = float(np.max(np.abs(q32 - q64)) / np.max(np.abs(q64)))
+        assert e <= max(TOL, GSPAT_SPREAD * e32), (
+            f"GS-PAT request {i} (M={len(r.foci)}): drive {e:.3e}, reference f32 {e32:.3e}")
         # the slice is the pressure field of the solved drive
         drive = gsrc.copy()
         drive[:, 6], drive[:, 7] = ap[0::2], ap[1::2]

@@ -312,3 +312,20 @@ def test_gs_and_naive_oracles_run():
         src, q = fn(1, w.sources, w.k, w.atten, foci, amps) if fn is O.naive_f64 else fn(
             1, w.sources, w.k, w.atten, foci, amps)
         assert np.all(np.isfinite(q))
+
+
+def test_gspat_f32_restatement_tracks_f64():
+    """The f32 GS-PAT restatement (the reference's own arithmetic) stays within 1e-4 of the
+    float64 one on well-separated foci, reaches the same focal amplitudes, and leaves
+    positions, directions and frequencies untouched."""
+    rng = np.random.default_rng(5)
+    w, foci, amps = W.gspat_request(rng, 6)
+    s32, q32 = O.gspat_f32(1, w.sources, w.k, w.atten, foci, amps)
+    s64, q64 = O.gspat_f64(1, w.sources, w.k, w.atten, foci, amps)
+    s32, s64 = s32.reshape(-1, 9), s64.reshape(-1, 9)
+    assert np.max(np.abs(q32 - q64)) <= 1e-4 * np.max(np.abs(q64))
+    np.testing.assert_allclose(s32[:, 6], np.abs(q32), rtol=1e-6)
+    p32 = np.abs(O.field_f64(1, s32, w.k, w.atten, foci))
+    p64 = np.abs(O.field_f64(1, s64, w.k, w.atten, foci))
+    assert np.max(np.abs(p32 - p64)) <= 1e-4 * np.max(p64)
+    np.testing.assert_array_equal(s32[:, [0, 1, 2, 3, 4, 5, 8]], w.sources[:, [0, 1, 2, 3, 4, 5, 8]])
