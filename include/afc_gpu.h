@@ -194,7 +194,9 @@ int32_t AFC_MeasurePipeRates(double rates[6], double *sm_clock_hz, int32_t *sm_c
 
 /* Select the device that calculators and solvers created afterwards on this thread use (the
  * reference's Vulkan calculator always takes the first device, gpu/gpu_calculator.rs:34-37;
- * the default here is also device 0).  The device-level calls follow their stream's device. */
+ * the default here is also device 0).  The device-level calls follow their stream's device;
+ * every call that launches on a device other than the thread's current one switches to it for
+ * the call and back before returning, so no call changes the caller's current device. */
 int32_t AFC_SetDevice(int32_t device);
 
 /* Number of CUDA devices visible to this library (0 when none or the driver is unusable). */
@@ -210,9 +212,10 @@ int32_t AFC_CudaDeviceCount(void);
  * reserves on every GPU it is loaded on, for the life of the process; inputs and output are
  * the caller's, as for AFC_FieldGridDevice.  More sources than AFC_NOALLOC_MAX_SOURCES are
  * rejected with AFC_ERR_TOO_LARGE.  The first call on each device looks the scratch address
- * up (make it before capturing the stream into a graph).  All calls share the one scratch
- * array, so calls whose GPU work overlaps (unordered streams) race; order them on one stream.
- * It calls no allocator. */
+ * up (make it before capturing the stream into a graph) and keeps it for the life of the
+ * process: use streams of the device's primary context and do not reset the device after that
+ * first call.  All calls share the one scratch array, so calls whose GPU work overlaps
+ * (unordered streams) race; order them on one stream.  It calls no allocator. */
 #define AFC_NOALLOC_MAX_SOURCES 16384
 int32_t AFC_FieldGridDeviceNoAlloc(int32_t source_type, int32_t field_type, int32_t sum_mode,
                                    const float *d_sources, const float *d_wavenums,

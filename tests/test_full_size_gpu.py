@@ -189,6 +189,7 @@ def test_serving_stream_at_load_same_alone_and_vs_oracle(gpu):
     gid, gsrc, gk, ga, cen = gs
     fields = [i for i, r in enumerate(stream) if r.kind == "field"]
     gspats = [i for i, r in enumerate(stream) if r.kind == "gspat"]
+    worst_field, worst_slice, gspat_ratio = 0.0, 0.0, []
     for i in rng.choice(fields, 40, replace=False):
         jb = pool[stream[i].job]
         got = _as_field(mixed[i][0], jb.field_type)
@@ -198,8 +199,9 @@ def test_serving_stream_at_load_same_alone_and_vs_oracle(gpu):
             p = O.grid_points(2, lo, hi, jb.grid.res, jb.grid.axes)[rows]
         else:
             p = pts_cache[stream[i].job][rows]
-        _check(got[rows], O.field_f32(1, jb.sources, jb.k, jb.atten, p), jb.field_type,
-               f"served field request {i}")
+        worst_field = max(worst_field, _check(got[rows],
+                                              O.field_f32(1, jb.sources, jb.k, jb.atten, p),
+                                              jb.field_type, f"served field request {i}"))
     big_first = sorted(gspats, key=lambda i: -len(stream[i].foci))
     for i in big_first[:4] + list(rng.choice(big_first[4:], 12, replace=False)):
         r = stream[i]
@@ -211,6 +213,7 @@ def test_serving_stream_at_load_same_alone_and_vs_oracle(gpu):
         e32 = float(np.max(np.abs(q32 - q64)) / np.max(np.abs(q64)))
         assert e <= max(TOL, GSPAT_SPREAD * e32), (
             f"GS-PAT request {i} (M={len(r.foci)}): drive {e:.3e}, reference f32 {e32:.3e}")
+        gspat_ratio.append((e, e32, len(r.foci)))
         # the slice is the pressure field of the solved drive
         drive = gsrc.copy()
         drive[:, 6], drive[:, 7] = ap[0::2], ap[1::2]
@@ -218,4 +221,8 @@ def test_serving_stream_at_load_same_alone_and_vs_oracle(gpu):
         lo, hi = spec.lo_hi()
         rows = np.sort(rng.choice(201 * 201, SAMPLE_POINTS, replace=False))
         p = O.grid_points(2, lo, hi, spec.res, spec.axes)[rows]
-        _check(slice_out[rows], O.field_f32(1, drive, gk, ga, p), 0, f"GS-PAT slice {i}")
+        worst_slice = max(worst_slice, _check(slice_out[rows], O.field_f32(1, drive, gk, ga, p),
+                                              0, f"GS-PAT slice {i}"))
+    print(f"serving stream: worst field {worst_field:.2e}, worst slice {worst_slice:.2e}, "
+          f"GS-PAT drive (gpu vs f64, reference f32 vs f64, M): "
+          f"{[(f'{a:.1e}', f'{b:.1e}', m) for a, b, m in sorted(gspat_ratio)[-5:]]}")
