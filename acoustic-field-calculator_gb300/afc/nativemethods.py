@@ -136,7 +136,8 @@ NEW_EXPORTS = [
     "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
     "AFC_MultiPatternWorkspaceBytes", "AFC_MultiPatternBuildG", "AFC_MultiPatternApply",
     "AFC_MultiPatternStatus", "AFC_MultiPatternDirect", "AFC_BatchCreate", "AFC_BatchRun",
-    "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchFree", "AFC_ServeCreate",
+    "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchDescribeKernels", "AFC_BatchFree",
+    "AFC_ServeCreate",
     "AFC_ServeAddGeometry", "AFC_ServeSubmitField", "AFC_ServeSubmitGspat", "AFC_ServeWait",
     "AFC_ServeStats", "AFC_ServeDestroy",
 ]
@@ -301,6 +302,10 @@ def __init_new():
     AFC_DLL.AFC_BatchDescribe.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32),
                                           POINTER(c_uint64), POINTER(c_double)]
     AFC_DLL.AFC_BatchDescribe.restype = c_int32
+    AFC_DLL.AFC_BatchDescribeKernels.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32),
+                                                 POINTER(c_uint64), POINTER(c_int32),
+                                                 POINTER(c_int32), POINTER(c_uint64)]
+    AFC_DLL.AFC_BatchDescribeKernels.restype = c_int32
     AFC_DLL.AFC_BatchFree.argtypes = [c_void_p]
     AFC_DLL.AFC_BatchFree.restype = None
     AFC_DLL.AFC_ServeCreate.argtypes = [POINTER(ServeConfig), POINTER(c_void_p)]

@@ -62,5 +62,13 @@ def describe(afc, plan):
     evals = ctypes.c_double()
     afc.DLL.AFC_BatchDescribe(plan, ctypes.byref(pairs), ctypes.byref(bps), ctypes.byref(items),
                               ctypes.byref(evals))
+    rp, rb, ri = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
+    fp, fb, fi = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
+    afc.DLL.AFC_BatchDescribeKernels(plan, ctypes.byref(rp), ctypes.byref(rb), ctypes.byref(ri),
+                                     ctypes.byref(fp), ctypes.byref(fb), ctypes.byref(fi))
     return {"pairs_per_thread": pairs.value, "blocks_per_sm": bps.value, "items": items.value,
-            "evals": evals.value}
+            "evals": evals.value,
+            "rows_kernel": {"pairs_per_thread": rp.value, "blocks_per_sm": rb.value,
+                            "items": ri.value},
+            "flat_kernel": {"pairs_per_thread": fp.value, "blocks_per_sm": fb.value,
+                            "items": fi.value}}

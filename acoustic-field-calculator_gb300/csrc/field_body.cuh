@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "afc_internal.h"
@@ -51,22 +52,75 @@ __device__ __forceinline__ PackedSource pack_source(int st, const float* __restr
 struct SmemTile {
     float4 v0[kTile], v1[kTile], v2[kTile], v3[kTile], v4[kTile];
     float2 ns[kTile];
-    float4 dir[kDirTableSize];    // theta-binned cubics (this body; the exact edge paths)
-    float cneg[kCTabSize];        // cos(theta)-indexed table of the rows body: -L per interval
-    float4 ccoef[2 * kCTabSize];  // and the cubic of each side
+    float4 dir[kDirTableSize];    // theta-binned cubics (the exact edge paths)
     float box[kThreads / 32][6];  // per-warp bounds of the block's points (min xyz, max xyz)
     float bbox[6];                // the block's bounds
+};
+
+// The rows body's cos(theta)-indexed table in shared memory.
+struct RowsTable {
+    float cneg[kCTabSize];        // -L per interval
+    float4 ccoef[2 * kCTabSize];  // the cubic of each side
+};
+
+// Shared memory of the rows kernels: the staging tile and the rows table in one object (the
+// layout the kernels' register allocation was tuned on; as two separate objects the 256^3
+// launch ran 2 % slower).
+struct RowsSmem {
+    SmemTile sm;
+    RowsTable rt;
 };
 
 // The cos(theta)-indexed directivity table in global memory (one copy per translation unit).
 static __device__ const float g_ctab_negedge[kCTabSize] = AFC_CTAB_NEGEDGE_INIT;
 static __device__ const float4 g_ctab_coef[2 * kCTabSize] = AFC_CTAB_COEF_INIT;
 
-// Fill the block's directivity tables (a __syncthreads must follow before their first use).
-__device__ __forceinline__ void load_dir_tables(SmemTile& sm, const float4* __restrict__ dir) {
+// Bytes of dynamic shared memory a general-body kernel needs for its GTable.
+constexpr int kGTableBytes = static_cast<int>(sizeof(GTable));
+
+// Dynamic shared memory beyond the default 48 KB per block needs an opt-in per kernel and per
+// device; it is made once per device (one bit per device of the first 64) before a launch.
+template <auto Kernel>
+cudaError_t allow_dynamic_smem(int bytes) {
+    static std::atomic<uint64_t> done{0};
+    if (bytes <= 0) return cudaSuccess;
+    int dev = 0;
+    const cudaError_t ge = cudaGetDevice(&dev);
+    if (ge != cudaSuccess) return ge;
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    const cudaError_t e =
+        cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+    return e;
+}
+
+// Fill the block's theta-binned table (a __syncthreads must follow before its first use).
+__device__ __forceinline__ void load_theta_table(SmemTile& sm, const float4* __restrict__ dir) {
     if (threadIdx.x < kDirTableSize) sm.dir[threadIdx.x] = dir[threadIdx.x];
-    for (int i = threadIdx.x; i < kCTabSize; i += blockDim.x) sm.cneg[i] = g_ctab_negedge[i];
-    for (int i = threadIdx.x; i < 2 * kCTabSize; i += blockDim.x) sm.ccoef[i] = g_ctab_coef[i];
+}
+
+// Fill the rows body's table (a __syncthreads must follow before its first use).
+__device__ __forceinline__ void load_rows_table(RowsTable& rt) {
+    for (int i = threadIdx.x; i < kCTabSize; i += blockDim.x) rt.cneg[i] = g_ctab_negedge[i];
+    for (int i = threadIdx.x; i < 2 * kCTabSize; i += blockDim.x) rt.ccoef[i] = g_ctab_coef[i];
+}
+
+// Fill the general body's lane-replicated table from the rows table's intervals (entry u is
+// interval u + BIAS - 1 there) and the clamp entry (edge at c = 1/2, D = 1 above, 0 below); a
+// __syncthreads must follow before its first use.
+__device__ __forceinline__ void load_gtab(GTable& g) {
+    constexpr int kFirst = AFC_CTAB_BIAS - 1;
+    for (int i = threadIdx.x; i < kGTabEntries * kGTabNegCopies; i += blockDim.x) {
+        const int u = i / kGTabNegCopies;
+        g.neg[i] = u < kGTabLast ? g_ctab_negedge[u + kFirst] : -0.5f;
+    }
+    for (int i = threadIdx.x; i < kGTabEntries * 2 * kGTabCoefCopies; i += blockDim.x) {
+        const int e = i / kGTabCoefCopies;  // 2u + side
+        const int u = e >> 1, side = e & 1;
+        g.coef[i] = u < kGTabLast ? g_ctab_coef[2 * (u + kFirst) + side]
+                                  : make_float4(side ? 0.f : 1.f, 0.f, 0.f, 0.f);
+    }
 }
 
 // The phase phi + k r goes to sin/cos.approx unreduced when it is at most this large for every
@@ -154,15 +208,18 @@ __device__ __forceinline__ float2 ref_dist2(float2 dx, float2 dy, float2 dz) {
     return make_float2(ref_dist2_1(dx.x, dy.x, dz.x), ref_dist2_1(dx.y, dy.y, dz.y));
 }
 
-// Correction for one point of a thread whose points include one next to a bin edge: recompute
-// the pair with the hot loop's operations (UD: cos(theta) from the shared direction); if its
-// fast theta is next to an edge and the reference's bin (exact_bin) differs from the fast one,
-// return w (D_exact - D_fast) (cos, sin), the amount to add to the point's accumulators, else
-// zero.  Everything passes by value so that the caller's accumulators stay in registers.
+// Correction for one point of a thread whose points include one next to a bin edge (or, in the
+// careful variant, possibly on a source's back axis): recompute the pair with the hot loop's
+// operations (UD: cos(theta) from the shared direction); if its fast cos(theta) is within
+// kCTabMargin of the edge of its table interval, or below kBackAxisC, return w (D_exact -
+// D_fast) (cos, sin), the amount to add to the point's accumulators, with D_exact the cubic of
+// the reference's bin (exact_bin) at the fast theta; else zero.  Everything passes by value so
+// that the caller's accumulators stay in registers.
 template <bool UD>
-__device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, float4 v0, float4 v1,
-                                               float4 v2, float4 v3, float4 v4, float2 ns,
-                                               float3 n0, float np, float px, float py, float pz) {
+__device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, GTableLane g,
+                                               float4 v0, float4 v1, float4 v2, float4 v3,
+                                               float4 v4, float2 ns, float3 n0, float np,
+                                               float px, float py, float pz) {
     const float dx = px + v0.x, dy = py + v0.z, dz = pz + v1.x;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float rinv = mufu_rsqrt(r2);
@@ -178,18 +235,16 @@ __device__ __noinline__ float2 edge_correction(const float4* __restrict__ tab, f
         ny = v2.z;
         nz = v3.x;
     }
-    float2 xc;
-    directivity2_fast(tab, make_float2(ct, ct), xc);
-    if (!near_edge(xc.x) && !(ct < kBackAxisC)) return make_float2(0.f, 0.f);
+    float2 t;
+    const float d_fast = directivity2_gtab(g, make_float2(ct, ct), t).x;
+    if (!near_edge_c(t.x) && !(ct < kBackAxisC)) return make_float2(0.f, 0.f);
     const float thc = theta2_centred(make_float2(ct, ct)).x;
-    const int i_fast = fast_bin(thc);
     const int i_exact = exact_bin(dx, dy, dz, nx, ny, nz);
-    if (i_exact == i_fast) return make_float2(0.f, 0.f);
     float2 r;
     const float red =
         ref_phase2(ref_dist2(f2(dx), f2(dy), f2(dz)), f2(rinv), f2(v1.z), f2(v4.z), r).x;
     const float w0 = rinv * mufu_ex2(fmaf(v3.z, r.x, v4.x));
-    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - dir_in_bin(tab, thc, i_fast));
+    const float corr = w0 * (dir_in_bin(tab, thc, i_exact) - d_fast);
     return make_float2(corr * mufu_cos(red), corr * mufu_sin(red));
 }
 
@@ -211,21 +266,20 @@ struct PairGeom {
 };
 
 // The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
-// records whether any of the thread's points has its theta next to a bin edge; that rare case
-// recomputes the pairs' geometry to find which points, and corrects them one by one.  RED:
-// the careful variant, for tiles with a large phase bound or with some point possibly behind a
-// source: the phase is rounded as the reference rounds it and reduced before sin/cos
-// (ref_phase2, kUnreducedPhaseMax), and a cos(theta) next to -1 (kBackAxisC) also takes the
-// exact path.  This body keeps the theta-binned
-// directivity (acos polynomial and MUFU square root): with three coordinates per point it has
-// no registers left for the cos(theta)-indexed table's two dependent lookups, which spill here
-// and made the batched kernel 12 % slower, while the rows body (field_rows.cuh) gains 8 %.
+// records the smallest distance of any of the thread's points to the bin edge of its table
+// interval; that rare case recomputes the pairs' geometry to find which points, and corrects
+// them one by one.  RED: the careful variant, for tiles with a large phase bound or with some
+// point possibly behind a source: the phase is rounded as the reference rounds it and reduced
+// before sin/cos (ref_phase2, kUnreducedPhaseMax), and a cos(theta) next to -1 (kBackAxisC)
+// also takes the exact path.  The directivity comes straight from cos(theta), from the
+// lane-replicated table (directivity2_gtab): no acos and no MUFU square root.
 template <int ST, int SUM, int PAIRS, bool UD, bool RED>
-__device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, float3 n0,
-                                                  float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
-                                                  float2 (&PZ)[PAIRS], float2 (&NP)[PAIRS],
-                                                  float2 (&RE)[PAIRS], float2 (&IM)[PAIRS],
-                                                  float2 (&CRE)[PAIRS], float2 (&CIM)[PAIRS]) {
+__device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTableLane& g, int j,
+                                                  float3 n0, float2 (&PX)[PAIRS],
+                                                  float2 (&PY)[PAIRS], float2 (&PZ)[PAIRS],
+                                                  float2 (&NP)[PAIRS], float2 (&RE)[PAIRS],
+                                                  float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                                  float2 (&CIM)[PAIRS]) {
     const float4 v0 = sm.v0[j], v1 = sm.v1[j], v3 = sm.v3[j], v4 = sm.v4[j];
     float4 v2 = make_float4(0.f, 0.f, 0.f, 0.f);
     float2 ns = f2(0.f);
@@ -233,7 +287,8 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         if constexpr (UD) ns = sm.ns[j];
         else v2 = sm.v2[j];
     }
-    bool any_near = false;
+    float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
+    bool any_back = false;         // careful variant: some c next to -1
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
@@ -245,10 +300,10 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
-            float2 xc;
-            w = mul2(w, directivity2_fast(sm.dir, p.ct, xc));
-            any_near |= near_edge(xc.x) | near_edge(xc.y);
-            if constexpr (RED) any_near |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
+            float2 t;
+            w = mul2(w, directivity2_gtab(g, p.ct, t));
+            near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
+            if constexpr (RED) any_back |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
         }
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
         const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
@@ -264,11 +319,11 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
         }
     }
     if constexpr (ST == SRC_T4010A1) {
-        if (any_near) {
+        if (near_min < kCTabMargin || any_back) {
 #pragma unroll
             for (int k = 0; k < 2 * PAIRS; ++k) {
                 const int q = k >> 1, h = k & 1;
-                const float2 c = edge_correction<UD>(sm.dir, v0, v1, v2, v3, v4, ns, n0,
+                const float2 c = edge_correction<UD>(sm.dir, g, v0, v1, v2, v3, v4, ns, n0,
                                                      lane_of(NP[q], h), lane_of(PX[q], h),
                                                      lane_of(PY[q], h), lane_of(PZ[q], h));
                 if constexpr (SUM == SUM_PLAIN) {
@@ -288,13 +343,15 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, int j, flo
 // their fields into RE, IM (CRE, CIM: compensation terms).  `grid` selects generated grid
 // points or explicit ones; source 0's direction is the shared direction of the fast cos(theta).
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSource* __restrict__ src,
+__device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
+                                                 const PackedSource* __restrict__ src,
                                                  int64_t n, int64_t s_lo, int64_t s_hi, bool grid,
                                                  const GridDev& g, const float* __restrict__ pts,
                                                  int64_t m, int64_t first, float2 (&RE)[PAIRS],
                                                  float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
                                                  float2 (&CIM)[PAIRS]) {
     constexpr int kPPT = 2 * PAIRS;
+    const GTableLane gl(gt);
     const int64_t base = first + threadIdx.x;
     float2 PX[PAIRS], PY[PAIRS], PZ[PAIRS], NP[PAIRS];
 #pragma unroll
@@ -403,24 +460,24 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const PackedSourc
             if (tile_plain) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, true, false>(sm, j, n0, PX, PY, PZ, NP, RE,
+                    accumulate_source<ST, SUM, PAIRS, true, false>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
                                                                    IM, CRE, CIM);
             } else {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, true, true>(sm, j, n0, PX, PY, PZ, NP, RE, IM,
+                    accumulate_source<ST, SUM, PAIRS, true, true>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
                                                                   CRE, CIM);
             }
         } else {
             if (tile_plain) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, false, false>(sm, j, n0, PX, PY, PZ, NP, RE,
+                    accumulate_source<ST, SUM, PAIRS, false, false>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
                                                                     IM, CRE, CIM);
             } else {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, false, true>(sm, j, n0, PX, PY, PZ, NP, RE,
+                    accumulate_source<ST, SUM, PAIRS, false, true>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
                                                                    IM, CRE, CIM);
             }
         }
@@ -519,12 +576,14 @@ __device__ __forceinline__ void block_store(float2 (&RE)[PAIRS], float2 (&IM)[PA
 // One block of 2*PAIRS*kThreads observation points starting at point `first`, all n sources:
 // accumulate, apply the field transform and store.
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void block_points(SmemTile& sm, const PackedSource* __restrict__ src,
-                                             int64_t n, bool grid, const GridDev& g,
+__device__ __forceinline__ void block_points(SmemTile& sm, const GTable& gt,
+                                             const PackedSource* __restrict__ src, int64_t n,
+                                             bool grid, const GridDev& g,
                                              const float* __restrict__ pts, int64_t m,
                                              int64_t first, int field, void* __restrict__ out) {
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    block_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE, CIM);
+    block_accumulate<ST, SUM, PAIRS>(sm, gt, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE,
+                                     CIM);
     block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, grid, g, pts, first, m, field, out);
 }
 

@@ -19,9 +19,11 @@
 //     are corrected after the source, off the interleaved path.
 //   * On grids with more than one point along the second axis a thread's points are
 //     consecutive along that axis (field_rows_kernel), so the offsets along the other two axes
-//     are computed once per source and thread.  That body takes the directivity from a
-//     cos(theta)-indexed table (no acos, no MUFU square root; propagate.cuh); the general body
-//     keeps the theta-binned one, whose temporaries its registers can hold.
+//     are computed once per source and thread.  Both bodies take the directivity from a
+//     cos(theta)-indexed table (no acos, no MUFU square root; propagate.cuh): the rows body
+//     from the plain table, whose entries neighbouring grid points share, the general body from
+//     a lane-replicated copy in dynamic shared memory that scattered points read without bank
+//     conflicts.
 //   * When every source of a tile points the same way as source 0 (a planar array), cos(theta)
 //     comes from n.x - n.s with n.x precomputed per point and n.s per source: two FP32
 //     operations per pair instead of four.  Each block decides this per tile.
@@ -49,15 +51,24 @@ using namespace fb;
 
 __constant__ float4 c_dir_table[kDirTableSize] = AFC_DIR_TABLE_INIT;
 
+// The general body's lane-replicated directivity table lives in dynamic shared memory
+// (kGTableBytes for T4010A1 sources, none for sphere sources).
+__device__ __forceinline__ GTable& dynamic_gtab() {
+    extern __shared__ __align__(16) unsigned char afc_dyn_smem[];
+    return *reinterpret_cast<GTable*>(afc_dyn_smem);
+}
+
 template <int ST, int SUM, bool GRID, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
     field_direct_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
                         const float* __restrict__ pts, int64_t m, int field,
                         void* __restrict__ out) {
     __shared__ SmemTile sm;
-    load_dir_tables(sm, c_dir_table);
+    GTable& gt = dynamic_gtab();
+    load_theta_table(sm, c_dir_table);
+    if constexpr (ST == SRC_T4010A1) load_gtab(gt);
     const int64_t first = static_cast<int64_t>(blockIdx.x) * (kThreads * 2 * PAIRS);
-    block_points<ST, SUM, PAIRS>(sm, src, n, GRID, g, pts, m, first, field, out);
+    block_points<ST, SUM, PAIRS>(sm, gt, src, n, GRID, g, pts, m, first, field, out);
 }
 
 // The partial sums of a cluster's blocks, combined into rank 0's: every rank writes its sums
@@ -131,14 +142,16 @@ __global__ void __launch_bounds__(kThreads, 2)
     namespace cg = cooperative_groups;
     __shared__ SmemTile sm;
     constexpr int kPPT = 2 * PAIRS;
-    load_dir_tables(sm, c_dir_table);
+    GTable& gt = dynamic_gtab();
+    load_theta_table(sm, c_dir_table);
+    if constexpr (ST == SRC_T4010A1) load_gtab(gt);
     const unsigned S = cg::this_cluster().num_blocks();
     const int64_t first = static_cast<int64_t>(blockIdx.x / S) * (kThreads * kPPT);
     int64_t s_lo, s_hi;
     rank_sources(n, s_lo, s_hi);
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    block_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, GRID, g, pts, m, first, RE, IM, CRE,
-                                     CIM);
+    block_accumulate<ST, SUM, PAIRS>(sm, gt, src, n, s_lo, s_hi, GRID, g, pts, m, first, RE, IM,
+                                     CRE, CIM);
     cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
     if (cg::this_cluster().block_rank() == 0)
         block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, GRID, g, pts, first, m, field,
@@ -153,14 +166,17 @@ __global__ void __launch_bounds__(kThreads, 2)
                             int tx_log2, int64_t tiles0, int64_t tiles1, int field,
                             void* __restrict__ out) {
     namespace cg = cooperative_groups;
-    __shared__ SmemTile sm;
-    load_dir_tables(sm, c_dir_table);
+    __shared__ RowsSmem rs;
+    SmemTile& sm = rs.sm;
+    RowsTable& rt = rs.rt;
+    load_theta_table(sm, c_dir_table);
+    load_rows_table(rt);
     const int64_t tile = blockIdx.x / cg::this_cluster().num_blocks();
     int64_t s_lo, s_hi;
     rank_sources(n, s_lo, s_hi);
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    rows_accumulate<ST, SUM, PAIRS>(sm, src, n, s_lo, s_hi, g, tx_log2, tiles0, tiles1, tile, RE,
-                                    IM, CRE, CIM);
+    rows_accumulate<ST, SUM, PAIRS>(sm, rt, src, n, s_lo, s_hi, g, tx_log2, tiles0, tiles1, tile,
+                                    RE, IM, CRE, CIM);
     cluster_combine<SUM, PAIRS>(sm, RE, IM, CRE, CIM);
     if (cg::this_cluster().block_rank() == 0)
         rows_store<SUM, PAIRS>(src, n, g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM,
@@ -173,9 +189,12 @@ template <int ST, int SUM, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
     field_rows_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g, int tx_log2,
                       int64_t tiles0, int64_t tiles1, int field, void* __restrict__ out) {
-    __shared__ SmemTile sm;
-    load_dir_tables(sm, c_dir_table);
-    block_rows<ST, SUM, PAIRS>(sm, src, n, g, tx_log2, tiles0, tiles1, blockIdx.x, field, out);
+    __shared__ RowsSmem rs;
+    SmemTile& sm = rs.sm;
+    RowsTable& rt = rs.rt;
+    load_theta_table(sm, c_dir_table);
+    load_rows_table(rt);
+    block_rows<ST, SUM, PAIRS>(sm, rt, src, n, g, tx_log2, tiles0, tiles1, blockIdx.x, field, out);
 }
 
 __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
@@ -196,20 +215,68 @@ std::atomic<int> g_num_sms[kSmCacheDevices] = {};
 constexpr int64_t kMaxClusterBlocks = 8;
 constexpr int64_t kSplitMinSources = 64;
 
-// Cluster width for a launch of `blocks` point tiles over n sources on `slots` resident
-// blocks: 1 when the launch fills its last wave to 93 % or more (large launches), else the
-// S <= 8 (each rank keeping >= kSplitMinSources sources) whose blocks * S best fill whole
-// waves, each extra rank charged 1 % for its set-up and the combine.
-int64_t split_width(int64_t blocks, int64_t n, int64_t slots) {
-    auto fill = [&](int64_t b) {
-        const int64_t waves = (b + slots - 1) / slots;
-        return static_cast<double>(b) / static_cast<double>(waves * slots);
+// Blocks of Kernel that can be resident at once: launched alone (S = 1) or in clusters of S
+// blocks, where the occupancy calculator's count of co-resident clusters also sees how clusters
+// pack into the GPCs (7-block clusters, for one, leave some slots of every GPC empty).  Cached
+// per device and S; 2 blocks per SM if the query fails.
+template <auto Kernel>
+int64_t resident_blocks(int64_t S, int dyn) {
+    static std::atomic<int> cache[kSmCacheDevices][kMaxClusterBlocks + 1];
+    if (S < 1 || S > kMaxClusterBlocks) return 2LL * num_sms();
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = kSmCacheDevices;
+    if (dev < kSmCacheDevices) {
+        const int v = cache[dev][S].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int64_t v = 0;
+    if (allow_dynamic_smem<Kernel>(dyn) == cudaSuccess) {
+        if (S == 1) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, Kernel, kThreads, dyn) ==
+                cudaSuccess)
+                v = static_cast<int64_t>(b) * num_sms();
+        } else {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(static_cast<unsigned>(S), 1, 1);
+            cfg.blockDim = dim3(kThreads, 1, 1);
+            cfg.dynamicSmemBytes = static_cast<size_t>(dyn);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = static_cast<unsigned>(S);
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int c = 0;
+            if (cudaOccupancyMaxActiveClusters(&c, Kernel, &cfg) == cudaSuccess)
+                v = static_cast<int64_t>(c) * S;
+        }
+    }
+    if (v <= 0) {
+        (void)cudaGetLastError();  // a failed query must not surface as the next launch's error
+        return 2LL * num_sms();
+    }
+    if (dev < kSmCacheDevices) cache[dev][S].store(static_cast<int>(v), std::memory_order_relaxed);
+    return v;
+}
+
+// Cluster width for a launch of `blocks` point tiles over n sources, slots(S) being the blocks
+// resident at once in clusters of S: 1 when the launch fills its last wave to 93 % or more
+// (large launches), else the S <= 8 (each rank keeping >= kSplitMinSources sources) whose
+// blocks * S best fill whole waves, each extra rank charged 1 % for its set-up and the combine.
+template <class Slots>
+int64_t split_width(int64_t blocks, int64_t n, Slots slots) {
+    auto fill = [](int64_t b, int64_t sl) {
+        const int64_t waves = (b + sl - 1) / sl;
+        return static_cast<double>(b) / static_cast<double>(waves * sl);
     };
-    if (blocks <= 0 || fill(blocks) >= 0.93) return 1;
+    if (blocks <= 0) return 1;
+    double best_score = fill(blocks, slots(1));
+    if (best_score >= 0.93) return 1;
     int64_t best = 1;
-    double best_score = fill(blocks);
     for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
-        const double score = fill(blocks * S) - 0.01 * static_cast<double>(S - 1);
+        const double score = fill(blocks * S, slots(S)) - 0.01 * static_cast<double>(S - 1);
         if (score > best_score + 1e-9) {
             best = S;
             best_score = score;
@@ -218,22 +285,31 @@ int64_t split_width(int64_t blocks, int64_t n, int64_t slots) {
     return best;
 }
 
+// Dynamic shared memory of a general-body kernel for source type ST.
+template <int ST>
+constexpr int gtab_bytes() {
+    return ST == SRC_T4010A1 ? kGTableBytes : 0;
+}
+
 template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
                          void* out, cudaStream_t s) {
+    constexpr int kDyn = gtab_bytes<ST>();
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
-    const int64_t want = 2LL * num_sms();
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
     if (!rows.use) {
         // flat numbering whose blocks would leave the last wave short (or the GPU part empty):
         // split each tile's sources over a cluster
-        const int64_t S = split_width(flat_blocks, n, want);
+        const int64_t S = split_width(flat_blocks, n, [](int64_t w) {
+            return w <= 1 ? resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn)
+                          : resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(w, kDyn);
+        });
         if (S >= 2 && flat_blocks * S <= 0x7fffffffLL) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(static_cast<unsigned>(flat_blocks * S), 1, 1);
             cfg.blockDim = dim3(kThreads, 1, 1);
-            cfg.dynamicSmemBytes = 0;
+            cfg.dynamicSmemBytes = kDyn;
             cfg.stream = s;
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -243,13 +319,18 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
             cfg.attrs = attr;
             cfg.numAttrs = 1;
             cudaError_t e;
-            if (ps.is_grid)
-                e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, true, PAIRS>, src, n,
-                                       ps.grid, static_cast<const float*>(nullptr), ps.m, field,
-                                       out);
-            else
-                e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, false, PAIRS>, src, n,
-                                       ps.grid, ps.pts, ps.m, field, out);
+            if (ps.is_grid) {
+                e = allow_dynamic_smem<field_split_kernel<ST, SUM, true, PAIRS>>(kDyn);
+                if (e == cudaSuccess)
+                    e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, true, PAIRS>, src, n,
+                                           ps.grid, static_cast<const float*>(nullptr), ps.m,
+                                           field, out);
+            } else {
+                e = allow_dynamic_smem<field_split_kernel<ST, SUM, false, PAIRS>>(kDyn);
+                if (e == cudaSuccess)
+                    e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, false, PAIRS>, src, n,
+                                           ps.grid, ps.pts, ps.m, field, out);
+            }
             count_launch();
             return e != cudaSuccess ? e : cudaGetLastError();
         }
@@ -258,7 +339,10 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         const RowsTiling& t = rows;
         if (t.use) {
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-            const int64_t S = split_width(t.blocks, n, want);
+            const int64_t S = split_width(t.blocks, n, [](int64_t w) {
+                return w <= 1 ? resident_blocks<field_rows_kernel<ST, SUM, PAIRS>>(1, 0)
+                              : resident_blocks<field_rows_split_kernel<ST, SUM, PAIRS>>(w, 0);
+            });
             if (S >= 2 && t.blocks * S <= 0x7fffffffLL) {
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3(static_cast<unsigned>(t.blocks * S), 1, 1);
@@ -286,33 +370,37 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     }
     const int64_t blocks = flat_blocks;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    cudaError_t e;
     if (ps.is_grid) {
-        field_direct_kernel<ST, SUM, true, PAIRS><<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(
+        if ((e = allow_dynamic_smem<field_direct_kernel<ST, SUM, true, PAIRS>>(kDyn)) != cudaSuccess)
+            return e;
+        field_direct_kernel<ST, SUM, true, PAIRS><<<static_cast<unsigned>(blocks), kThreads, kDyn, s>>>(
             src, n, ps.grid, nullptr, ps.m, field, out);
     } else {
-        field_direct_kernel<ST, SUM, false, PAIRS><<<static_cast<unsigned>(blocks), kThreads, 0, s>>>(
+        if ((e = allow_dynamic_smem<field_direct_kernel<ST, SUM, false, PAIRS>>(kDyn)) != cudaSuccess)
+            return e;
+        field_direct_kernel<ST, SUM, false, PAIRS><<<static_cast<unsigned>(blocks), kThreads, kDyn, s>>>(
             src, n, ps.grid, ps.pts, ps.m, field, out);
     }
     count_launch();
     return cudaGetLastError();
 }
 
-// Points per thread.  Scatter points and single-row grids: the most that still gives every SM
-// two blocks (more points per thread amortise the shared-memory reads; too few blocks leave SMs
-// idle).  Grids with more than one point along their second axis, whose rows body shares two
-// coordinates per thread: 4 point pairs from 131,072 points and 2
-// from 32,768, the cluster split refilling the waves (measured: 40^3, 64^3 and 80^3 grids 4-9 %
-// faster than with the scatter thresholds; for scatter sets the same change was slower at
-// 131,072 and 262,144 points).
+// Points per thread, the cluster split refilling the waves.  Grids with more than one point
+// along their second axis, whose rows body shares two coordinates per thread: 4 point pairs
+// from 131,072 points and 2 from 32,768 (40^3, 64^3 and 80^3 grids ran 4-9 % faster than with
+// fewer pairs).  Scatter points and single-row grids: 4 point pairs from 32,768 points, one
+// below (3,984 sources: 65,536 points ran 24 % and 262,144 points 2 % faster with 4 pairs
+// than with one; 16,384 points ran 40 % slower with 2 pairs than with one, its 16 tiles too
+// few even split 8 ways).
 template <int ST>
 cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
                       int field, void* out, cudaStream_t s) {
     if (sum_mode == SUM_COMPENSATED)
         return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s);
-    const int64_t want = 2LL * num_sms();
     const bool rows_grid = ps.is_grid && ps.grid.count[1] > 1;  // the rows body can take it
-    const int64_t four_from = rows_grid ? 131072 : want * kThreads * 8;
-    const int64_t two_from = rows_grid ? 32768 : want * kThreads * 4;
+    const int64_t four_from = rows_grid ? 131072 : 32768;
+    const int64_t two_from = rows_grid ? 32768 : INT64_MAX;
     if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s);
     if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s);
     return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s);

@@ -109,7 +109,8 @@ static __device__ __noinline__ float2 edge_correction_rows(const float4* __restr
 // third grid axes; U: its points' coordinates along the second; n0a: the shared direction (of
 // source 0) in grid axis order, which every source of a UD tile has.
 template <int ST, int SUM, int PAIRS, bool UD, bool RED>
-__device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float p0, float p2,
+__device__ __forceinline__ void accumulate_rows(const SmemTile& sm, const RowsTable& rt, int j,
+                                                float p0, float p2,
                                                 int a0, int a1, float3 n0a, float2 (&U)[PAIRS],
                                                 float2 (&NP)[PAIRS], float2 (&RE)[PAIRS],
                                                 float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
@@ -147,7 +148,7 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
         if constexpr (ST == SRC_T4010A1) {
             float2 t;
-            w = mul2(w, directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t));
+            w = mul2(w, directivity2_ctab(rt.cneg, rt.ccoef, p.ct, t));
             near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
         }
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
@@ -171,12 +172,12 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, int j, float
             for (int q = 0; q < PAIRS; ++q) {
                 const RowGeom<UD> p(U[q], NP[q], sh, v0, v2, ns);
                 float2 t;
-                directivity2_ctab(sm.cneg, sm.ccoef, p.ct, t);
+                directivity2_ctab(rt.cneg, rt.ccoef, p.ct, t);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     if (!near_edge_c(lane_of(t, h))) continue;
                     const float2 c = edge_correction_rows(
-                        sm.dir, sm.cneg, sm.ccoef, lane_of(p.du, h), sh.dv, sh.dw, sh.vw2, lane_of(p.cn, h), n_a0,
+                        sm.dir, rt.cneg, rt.ccoef, lane_of(p.du, h), sh.dv, sh.dw, sh.vw2, lane_of(p.cn, h), n_a0,
                         n_a1, n_a2, a0, a1, v1.z, v4.z, v3.z, v4.x);
                     if constexpr (SUM == SUM_PLAIN) {
                         lane_of(RE[q], h) += c.x;
@@ -202,7 +203,8 @@ __device__ __forceinline__ float axis_coord(const GridDev& g, int k, int a, int6
 // of sources s_lo .. s_hi - 1 at the thread's points, in RE, IM (CRE, CIM: compensations).
 // Source 0's direction is the shared direction of the fast cos(theta) whatever the range.
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void rows_accumulate(SmemTile& sm, const PackedSource* __restrict__ src,
+__device__ __forceinline__ void rows_accumulate(SmemTile& sm, const RowsTable& rt,
+                                                const PackedSource* __restrict__ src,
                                                 int64_t n, int64_t s_lo, int64_t s_hi,
                                                 const GridDev& g, int tx_log2, int64_t tiles0,
                                                 int64_t tiles1, int64_t tile, float2 (&RE)[PAIRS],
@@ -314,24 +316,24 @@ __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const PackedSource
             if (tile_small) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, true, false>(sm, j, p0, p2, a0, a1, n0a, U, NP, RE,
+                    accumulate_rows<ST, SUM, PAIRS, true, false>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
                                                                  IM, CRE, CIM);
             } else {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, true, true>(sm, j, p0, p2, a0, a1, n0a, U, NP, RE,
+                    accumulate_rows<ST, SUM, PAIRS, true, true>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
                                                                 IM, CRE, CIM);
             }
         } else {
             if (tile_small) {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, false, false>(sm, j, p0, p2, a0, a1, n0a, U, NP,
+                    accumulate_rows<ST, SUM, PAIRS, false, false>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
                                                                   RE, IM, CRE, CIM);
             } else {
 #pragma unroll 1
                 for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, false, true>(sm, j, p0, p2, a0, a1, n0a, U, NP, RE,
+                    accumulate_rows<ST, SUM, PAIRS, false, true>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
                                                                  IM, CRE, CIM);
             }
         }
@@ -387,13 +389,14 @@ __device__ __forceinline__ void rows_store(const PackedSource* __restrict__ src,
 
 // One tile of the rows tiling, all n sources, stored.
 template <int ST, int SUM, int PAIRS>
-__device__ __forceinline__ void block_rows(SmemTile& sm, const PackedSource* __restrict__ src,
-                                           int64_t n, const GridDev& g, int tx_log2,
-                                           int64_t tiles0, int64_t tiles1, int64_t tile,
-                                           int field, void* __restrict__ out) {
+__device__ __forceinline__ void block_rows(SmemTile& sm, const RowsTable& rt,
+                                           const PackedSource* __restrict__ src, int64_t n,
+                                           const GridDev& g, int tx_log2, int64_t tiles0,
+                                           int64_t tiles1, int64_t tile, int field,
+                                           void* __restrict__ out) {
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    rows_accumulate<ST, SUM, PAIRS>(sm, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE, IM,
-                                    CRE, CIM);
+    rows_accumulate<ST, SUM, PAIRS>(sm, rt, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE,
+                                    IM, CRE, CIM);
     rows_store<SUM, PAIRS>(src, n, g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field,
                            out);
 }

@@ -295,6 +295,69 @@ __device__ __forceinline__ float2 directivity2_ctab(const float* __restrict__ ne
 
 __device__ __forceinline__ bool near_edge_c(float t) { return fabsf(t) < kCTabMargin; }
 
+// ------------------------------------------------------------------ the same, for scattered points
+//
+// The general body (scatter points, flat grids) takes D from the same cubics, laid out so that
+// the 32 lanes of a warp never meet in a shared-memory bank, whatever intervals their points
+// fall in.  The rows body's lanes hold neighbouring grid points and read a few neighbouring
+// entries; a warp of scattered points reads up to 32 different ones, and in the plain table
+// those collide in the banks (65,536- and 262,144-point launches ran 61 % and 54 % slower with
+// it than with the theta path, whose 32-entry table they then kept, at one MUFU square root
+// per pair).
+//   * Entry u = floor(K c) + 1 for c in [-1/K, (kGTabLast - 1)/K) (interval u + BIAS - 1 of the
+//     rows table), and u = kGTabClamp for every other c, taken with one unsigned minimum: c
+//     below -1/K (beyond 90 degrees: D = 0), c from (kGTabLast - 1)/K = 0.9453 up (below 19
+//     degrees, or a cosine rounded above 1: D = 1), and non-finite c.  The clamp entry's edge
+//     sits at c = 1/2 with D = 0 below and 1 above, which gives both.  Interval 0 holds the
+//     90-degree edge (its threshold is -2.2e-7) and interval kGTabLast - 1 the 20-degree one.
+//   * Edge thresholds: kGTabNegCopies copies interleaved word by word, lane l reading copy l: a
+//     warp's 32 four-byte loads fall in 32 different banks.
+//   * Cubics: kGTabCoefCopies copies interleaved 16 bytes by 16 bytes, lane l reading copy
+//     l mod 8: the 8 lanes of each phase of a 16-byte load fall in 8 different bank quads.
+// Points on a tilted source's back axis (c rounded below -1, D = 1 in the reference) clamp to
+// D = 0 here; the careful variant of the general body flags them (kBackAxisC) for the exact
+// path, as before.
+constexpr int kGTabLast = 122;               // entries 0 .. kGTabLast - 1 are table intervals
+constexpr unsigned kGTabClamp = kGTabLast;   // every other c
+constexpr int kGTabEntries = kGTabLast + 1;
+constexpr int kGTabNegCopies = 32;
+constexpr int kGTabCoefCopies = 8;
+// RD(c K + 2^23 + 1) = 2^23 + 1 + floor(c K) for c >= -1/K; below, the sum falls under 2^23 and
+// its bits under 0x4B000000, which the unsigned difference turns into a huge index.
+constexpr float kGTabMagic = 8388609.0f;
+constexpr unsigned kGTabBits = 0x4B000000u;
+
+struct GTable {
+    float neg[kGTabEntries * kGTabNegCopies];         // -L of entry u, copy l at u * 32 + l
+    float4 coef[kGTabEntries * 2 * kGTabCoefCopies];  // side s of entry u, copy l at (2u + s) * 8 + l
+};
+
+// The lane's views of the table (its copies).
+struct GTableLane {
+    const float* neg;
+    const float4* coef;
+    __device__ __forceinline__ explicit GTableLane(const GTable& g) {
+        const int lane = static_cast<int>(threadIdx.x & 31u);
+        neg = g.neg + lane;
+        coef = g.coef + (lane & (kGTabCoefCopies - 1));
+    }
+};
+
+// D of two scattered points from their fast cos(theta); t receives c - L (|t| < kCTabMargin:
+// next to a bin edge).  The same operations as directivity2_ctab on the table's intervals.
+__device__ __forceinline__ float2 directivity2_gtab(const GTableLane& g, float2 ct, float2& t) {
+    const float2 fq = __ffma2_rd(ct, f2(static_cast<float>(kCTabK)), f2(kGTabMagic));
+    const float2 nfi = fma2(fq, f2(-1.0f), f2(kGTabMagic));          // -floor(c K)
+    const float2 x = fma2(ct, f2(static_cast<float>(kCTabK)), nfi);  // c K - floor(c K)
+    const unsigned ux = min(__float_as_uint(fq.x) - kGTabBits, kGTabClamp);
+    const unsigned uy = min(__float_as_uint(fq.y) - kGTabBits, kGTabClamp);
+    t = add2(ct, make_float2(g.neg[ux * kGTabNegCopies], g.neg[uy * kGTabNegCopies]));
+    const float4 a = g.coef[((ux << 1) | (__float_as_uint(t.x) >> 31)) * kGTabCoefCopies];
+    const float4 b = g.coef[((uy << 1) | (__float_as_uint(t.y) >> 31)) * kGTabCoefCopies];
+    return make_float2(fmaf(fmaf(fmaf(a.w, x.x, a.z), x.x, a.y), x.x, a.x),
+                       fmaf(fmaf(fmaf(b.w, x.y, b.z), x.y, b.y), x.y, b.x));
+}
+
 // Directivity of two points with the exact path applied in place (used where the pair is not
 // on the hot loop).
 __device__ __forceinline__ float2 directivity2(const float4* __restrict__ tab, float2 ct, float2 dx,

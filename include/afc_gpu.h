@@ -109,11 +109,13 @@ int32_t AFC_MultiPatternDirect(int32_t source_type, const float *d_sources,
  * reference, which evaluates one AFC_Calculate at a time) ----
  *
  * A plan binds a list of jobs -- each one field evaluation of its own sources on its own grid
- * or points into its own output -- to a CUDA graph that packs every job's sources and runs one
- * persistent kernel over all (job, point block) work items, longest first.  The caller may
- * rewrite the contents of the source arrays between runs; the pointers and sizes are fixed at
- * creation.  `tune` != 0 times the candidate point tiles (1, 2, 4 point pairs per thread) on
- * the batch and keeps the fastest.  All jobs of a plan have the same source type. */
+ * or points into its own output -- to a CUDA graph that packs every job's sources and runs two
+ * persistent kernels over the (job, point tile) work items, longest first: one for the grid
+ * jobs that take the rows tiling, one for the others.  The caller may rewrite the contents of
+ * the source arrays between runs; the pointers and sizes are fixed at creation.  `tune` != 0
+ * times, on the batch itself, each kernel's point tile (1, 2, 4 point pairs per thread) and
+ * resident blocks per SM, and the plan with every grid job on the general kernel, and keeps
+ * the fastest.  All jobs of a plan have the same source type. */
 typedef struct AfcFieldJob {
     uint64_t n_sources;
     const float *d_sources; /* ABI records (AfcT4010A1 / AfcSphereWaveSource) */
@@ -133,9 +135,15 @@ int32_t AFC_BatchCreate(int32_t source_type, const AfcFieldJob *jobs, uint64_t n
 int32_t AFC_BatchRun(void *plan, void *stream);
 /* The same jobs launched one at a time (pack + field kernel per job), for comparison. */
 int32_t AFC_BatchRunOneByOne(void *plan, void *stream);
-/* Chosen point pairs per thread, resident CTAs per SM, work items, total evaluations. */
+/* The general kernel's point pairs per thread and resident CTAs per SM, the work items of
+ * both kernels, total evaluations. */
 int32_t AFC_BatchDescribe(void *plan, int32_t *pairs, int32_t *blocks_per_sm, uint64_t *items,
                           double *evals);
+/* Each kernel's point pairs per thread, resident CTAs per SM and work items (rows kernel: grid
+ * jobs on the rows tiling; flat kernel: the others).  Any pointer may be NULL. */
+int32_t AFC_BatchDescribeKernels(void *plan, int32_t *rows_pairs, int32_t *rows_blocks_per_sm,
+                                 uint64_t *rows_items, int32_t *flat_pairs,
+                                 int32_t *flat_blocks_per_sm, uint64_t *flat_items);
 void AFC_BatchFree(void *plan);
 
 /* ---- serving engine (no counterpart in the reference, whose calls block) ----
