@@ -108,18 +108,38 @@ __device__ __forceinline__ void load_rows_table(RowsTable& rt) {
 
 // Fill the general body's lane-replicated table from the rows table's intervals (entry u is
 // interval u + BIAS - 1 there) and the clamp entry (edge at c = 1/2, D = 1 above, 0 below); a
-// __syncthreads must follow before its first use.
+// __syncthreads must follow before its first use.  Blocks of kThreads threads: each thread
+// issues all its global loads before its first store, so the fill costs one load latency, not
+// one per element (as a strided loop it took a sizeable part of a short block).
 __device__ __forceinline__ void load_gtab(GTable& g) {
     constexpr int kFirst = AFC_CTAB_BIAS - 1;
-    for (int i = threadIdx.x; i < kGTabEntries * kGTabNegCopies; i += blockDim.x) {
-        const int u = i / kGTabNegCopies;
-        g.neg[i] = u < kGTabLast ? g_ctab_negedge[u + kFirst] : -0.5f;
+    constexpr int kNeg = kGTabEntries * kGTabNegCopies;
+    constexpr int kCoef = kGTabEntries * 2 * kGTabCoefCopies;
+    constexpr int kNegIt = (kNeg + kThreads - 1) / kThreads;
+    constexpr int kCoefIt = (kCoef + kThreads - 1) / kThreads;
+    float nv[kNegIt];
+    float4 cv[kCoefIt];
+#pragma unroll
+    for (int k = 0; k < kNegIt; ++k) {
+        const int u = static_cast<int>(threadIdx.x + k * kThreads) / kGTabNegCopies;
+        nv[k] = u < kGTabLast ? g_ctab_negedge[u + kFirst] : -0.5f;
     }
-    for (int i = threadIdx.x; i < kGTabEntries * 2 * kGTabCoefCopies; i += blockDim.x) {
-        const int e = i / kGTabCoefCopies;  // 2u + side
+#pragma unroll
+    for (int k = 0; k < kCoefIt; ++k) {
+        const int e = static_cast<int>(threadIdx.x + k * kThreads) / kGTabCoefCopies;  // 2u + side
         const int u = e >> 1, side = e & 1;
-        g.coef[i] = u < kGTabLast ? g_ctab_coef[2 * (u + kFirst) + side]
-                                  : make_float4(side ? 0.f : 1.f, 0.f, 0.f, 0.f);
+        cv[k] = u < kGTabLast ? g_ctab_coef[2 * (u + kFirst) + side]
+                              : make_float4(side ? 0.f : 1.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < kNegIt; ++k) {
+        const int i = static_cast<int>(threadIdx.x + k * kThreads);
+        if (i < kNeg) g.neg[i] = nv[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kCoefIt; ++k) {
+        const int i = static_cast<int>(threadIdx.x + k * kThreads);
+        if (i < kCoef) g.coef[i] = cv[k];
     }
 }
 
