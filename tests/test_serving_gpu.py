@@ -133,8 +133,10 @@ def test_gspat_request_matches_the_optimizer_call(gpu):
 def test_hbm_budget_limits_admission(gpu):
     afc = gpu
     geoms = _geometries()
-    # room for one 40x40-point complex field request of the 996-source geometry at a time
-    one = 256 * 4 + 8 * 996 + 48 * 996 + 8 * 1681 + 4096
+    # room for one 41x41-point complex field request of the 996-source geometry at a time: its
+    # drive, packed sources and result, and the partial sums of its 7 source chunks (a request
+    # that small is cut into chunks of at least 128 sources to spread over the GPU)
+    one = 256 * 4 + 8 * 996 + 48 * 996 + 8 * 1681 + 8 * 7 * 1681 + 4096
     eng = SC.Engine(afc, one, 1 << 26, 8)
     try:
         gid = eng.add_geometry(1, *geoms[1])
