@@ -76,11 +76,13 @@ def parse():
                          "the headline (single focus end to end, multi-pattern, batch, "
                          "serving)")
     ap.add_argument("--workload", default="grid",
-                    choices=["grid", "multipattern", "batch", "serving"],
+                    choices=["grid", "multipattern", "batch", "serving", "scatter"],
                     help="grid: the headline 256^3 field; multipattern: 1,024 patterns on "
                          "262,144 points through the tensor-core contraction; batch: 2,048 "
                          "uneven jobs in one persistent launch from a CUDA graph; serving: a "
-                         "Poisson request stream swept over arrival rates")
+                         "Poisson request stream swept over arrival rates; scatter: the "
+                         "3,984-source field at --scatter-points scattered points (the "
+                         "general body)")
     ap.add_argument("--lams", default="100,300,1000,3000,10000",
                     help="serving: arrival rates (req/s) of the sweep")
     # smaller cases of the same kernels (profiling); the defaults are the workloads above
@@ -88,6 +90,8 @@ def parse():
     ap.add_argument("--mp-points", type=int, default=262144, help="multipattern: points")
     ap.add_argument("--mp-patterns", type=int, default=1024, help="multipattern: patterns")
     ap.add_argument("--batch-jobs", type=int, default=2048, help="batch: job count")
+    ap.add_argument("--scatter-points", type=int, default=262144,
+                    help="scatter: points, drawn uniformly in the multi-pattern box")
     ap.add_argument("--serve-slots", type=int, default=32,
                     help="serving: requests in flight on the GPU at most")
     return ap.parse_args()
@@ -420,6 +424,80 @@ def run_ours(args):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ scatter points
+
+def run_scatter(args):
+    """The general (scatter-point) body alone: the 3,984-source large-grid geometry on
+    --scatter-points points drawn uniformly in a 200 x 200 x 150 mm box over the array (seed 7),
+    complex field, through the device-level AFC_FieldScatterDevice with everything resident;
+    the L2 is flushed between timed steps.  Roofline: the FP32 + MUFU bound measured on this GPU,
+    as for the headline."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    import afc
+
+    lib = afc.DLL
+    lib.AFC_SetDevice(local)
+    w = W.large_grid()
+    m = args.scatter_points
+    pts = W.scatter_box(7, m, W.array_center(w.sources[:, :3])[:2])
+    dev = torch.device("cuda", local)
+    d_src = torch.from_numpy(w.sources.reshape(-1)).to(dev)
+    d_k = torch.from_numpy(w.k).to(dev)
+    d_a = torch.from_numpy(w.atten).to(dev)
+    d_pts = torch.from_numpy(pts.reshape(-1)).to(dev)
+    ws_bytes = lib.AFC_FieldWorkspaceBytes(w.n)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    out = torch.empty(2 * m, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rc = lib.AFC_FieldScatterDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(), d_a.data_ptr(),
+                                        w.n, d_pts.data_ptr(), m, out.data_ptr(), ws.data_ptr(),
+                                        ws_bytes, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(afc.last_error())
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    rates = (ctypes.c_double * 6)()
+    clk = ctypes.c_double()
+    nsm = ctypes.c_int32()
+    if lib.AFC_MeasurePipeRates(rates, ctypes.byref(clk), ctypes.byref(nsm)) != 0:
+        raise RuntimeError(afc.last_error())
+    ts = []
+    launches0 = lib.AFC_KernelLaunchCount()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    launches = lib.AFC_KernelLaunchCount() - launches0
+    t = statistics.median(ts)
+    evals = w.n * m
+    mufu_bound = 1.0 / sum(1.0 / rates[i] for i in range(5))
+    peak = min(mufu_bound, rates[5] / FP32_PER_EVAL)
+    line = {"metric": "source-point evaluations/s (FP32 direct summation, scatter points)",
+            "value": evals / t, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"scatter_{w.n}src_{m}pts_complex", "sources": w.n,
+                       "points": m, "l2": "flushed between timed steps (256 MiB write)"},
+            "roofline": {"bound": "fp32+sfu issue (compute)", "achieved": evals / t,
+                         "peak": peak, "unit": "evals/s", "frac": evals / t / peak,
+                         "peak_source": "measured here (AFC_MeasurePipeRates), as the headline"},
+            "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ shared timing helper
@@ -886,6 +964,8 @@ def main():
         run_batch(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "scatter":
+        run_scatter(args)
     else:
         run_ours(args)
 
