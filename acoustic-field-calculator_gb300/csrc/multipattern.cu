@@ -19,20 +19,34 @@
 //   FP16 row-scaled: each row of G scaled by a power of two so that its largest entry is ~1,
 //     one FP16 GEMM, the scale undone in the epilogue (exact).
 //
-// GEMM kernel (one CTA per 128 x 256 output tile, 192 threads):
-//   warp 0 lane 0  TMA producer: 128 x 64 A and 256 x 64 B tiles (128-byte swizzle) into a
-//                  4-stage shared-memory ring, completion signalled on the stage's mbarrier.
-//   warp 1         allocates 256 TMEM columns; lane 0 issues tcgen05.mma (M=128, N=256, K=16,
-//                  FP32 accumulate in TMEM) and frees each stage with tcgen05.commit.
-//   warps 2-5      epilogue: tcgen05.ld of their 32 TMEM lanes, FP32 stores of C.
-// Every mbarrier wait is bounded; on time-out the CTA records an error code, drains its own
-// copies (bounded) and frees its tensor memory before it returns.
+// GEMM kernel (persistent, CTA pairs: clusters of 2 CTAs, one CTA per SM, 192 threads each):
+//   an output tile is 256 x 256; CTA rank r of the pair owns rows 128 r .. 128 r + 127 of the
+//   tile, loads those 128 rows of A and rows 128 r .. 128 r + 127 of the tile's 256 B^T rows,
+//   and holds its 128 rows x 256 columns of the accumulator in its own tensor memory.
+//   warp 0 lane 0  TMA producer (both CTAs): per 64-wide K block its A plane(s) and B^T
+//                  plane(s), 128 x 64 each, 128-byte swizzle, into a shared-memory ring
+//                  (split BF16: A hi, A lo, B hi, B lo = 64 KB a stage, 3 stages; FP16:
+//                  32 KB, 7 stages) that runs on across tiles.  Both CTAs' copies complete on
+//                  the rank-0 CTA's stage barrier.
+//   warp 1         allocates 512 TMEM columns in both CTAs (two 256-column accumulators); in
+//                  the rank-0 CTA lane 0 issues tcgen05.mma.cta_group::2 (M = 256, N = 256,
+//                  K = 16, FP32 accumulate) -- split BF16 interleaves hi*hi, hi*lo and lo*hi
+//                  within each K block, so every operand plane is read once per tile -- and
+//                  frees each stage in both CTAs with one multicast tcgen05.commit.
+//   warps 2-5      epilogue (both CTAs): tcgen05.ld of their 32 TMEM lanes, FP32 stores of C,
+//                  overlapping the next tile's MMAs in the other accumulator.
+// Per SM and K block this moves 32 (FP16) or 64 KB (split BF16) for 4 or 12 MMA steps of
+// 128 x 256 x 16, two thirds (FP16) or four ninths (split BF16) of the operand bytes a 128 x 256
+// single-CTA tile reads for the same work.
+// Every mbarrier wait is bounded; on time-out the CTA records an error code, lets its copies in
+// flight land (bounded) and frees its tensor memory before it returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -44,16 +58,25 @@
 namespace afc {
 namespace mp {
 
-constexpr int BM = 128;
-constexpr int BN = 256;
-constexpr int BK = 64;  // 64 x 2-byte elements = one 128-byte swizzle row
-constexpr int STAGES = 4;
-constexpr int A_TILE = BM * BK * 2;
-constexpr int B_TILE = BN * BK * 2;
-constexpr int STAGE_BYTES = A_TILE + B_TILE;
+constexpr int BM = 256;    // output tile rows (a CTA pair)
+constexpr int BN = 256;    // output tile columns
+constexpr int BK = 64;     // 64 x 2-byte elements = one 128-byte swizzle row
+constexpr int HALF = 128;  // rows of A and of B^T that one CTA of the pair loads per tile
+constexpr int OP_TILE = HALF * BK * 2;  // 16 KB: 128 rows of one K block of one operand plane
 constexpr int GEMM_THREADS = 192;
 constexpr int TMEM_COLS = 256;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+// Shared-memory ring of the GEMM: per stage kPlanes A tiles then kPlanes B^T tiles.
+template <bool BF16>
+struct GemmCfg {
+    static constexpr int kPlanes = BF16 ? 2 : 1;  // split BF16: hi and lo
+    static constexpr int kStageBytes = 2 * kPlanes * OP_TILE;
+    static constexpr int kStages = BF16 ? 3 : 7;
+    static constexpr int kSmemBytes = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+};
+static_assert(GemmCfg<true>::kSmemBytes <= 227 * 1024 && GemmCfg<false>::kSmemBytes <= 227 * 1024,
+              "GEMM ring exceeds the shared memory of a CTA");
+static_assert((2 * GemmCfg<false>::kStages + 5) * 8 + 8 <= 256, "GEMM barriers exceed their area");
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 enum : unsigned { ERR_NONE = 0, ERR_TIMEOUT_PRODUCER = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_EPILOGUE = 3 };
@@ -93,12 +116,40 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int c0, int c1) {
+// Shared::cluster address of the same shared-memory object in the CTA of the given cluster rank.
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Every thread of both CTAs of the cluster; orders shared and global memory across them.
+__device__ __forceinline__ void cluster_sync() {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        "barrier.cluster.arrive.release.aligned;\n\t"
+        "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Arrive on an mbarrier given by its shared::cluster address (this CTA's or the peer's).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// TMA 2-D tile load into this CTA's shared memory; the transaction bytes complete on the mbarrier
+// at shared::cluster address `bar`, which may lie in the peer CTA of the pair.
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t bar,
+                                                 int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
         " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1)
         : "memory");
 }
 
@@ -131,19 +182,25 @@ __host__ __device__ constexpr uint32_t mma_idesc(bool bf16) {
            (static_cast<uint32_t>(BN >> 3) << 17) | (static_cast<uint32_t>(BM >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t adesc, uint64_t bdesc,
-                                        uint32_t idesc, uint32_t accumulate) {
+// One M = 256 step over the CTA pair: A rows 0-127 and B^T rows 0-127 from this (rank-0) CTA's
+// shared memory, rows 128-255 from the same offsets in the peer's; D rows 0-127 in this CTA's
+// tensor memory, rows 128-255 at the same address in the peer's.
+__device__ __forceinline__ void mma_f16_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc,
+                                             uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+// Arrive once on the mbarrier at this offset in both CTAs of the pair when every tcgen05
+// operation this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
     asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(bar))
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+        " [%0], %1;" ::"r"(smem_u32(bar)),
+        "h"(static_cast<uint16_t>(3))
         : "memory");
 }
 
@@ -165,146 +222,214 @@ __device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, uint32_t (&v)[32]
 // ------------------------------------------------------------------ GEMM
 
 struct GemmArgs {
-    int k_blocks;        // BK-blocks per segment
-    int nseg;            // 1 (FP16) or 3 (split BF16)
-    int seg_a[3];        // which A map each segment reads (0 hi, 1 lo)
-    int seg_b[3];        // which B map each segment reads
+    int k_blocks;        // BK-blocks of the contraction (kpad / BK)
     float* c;            // M x ldc floats
     int64_t ldc;         // row stride of C in floats
     int64_t m;           // rows of C
+    int n_tiles;         // BN-wide column tiles of C
+    int64_t tiles;       // output tiles in all (BM-row tiles x n_tiles)
     const float* row_scale;  // nullable: C row i multiplied by row_scale[i]
     unsigned* err;       // error code (first writer wins)
 };
 
+// Persistent: CTA pair p computes output tiles p, p + pairs, ... (tile t = row tile t / n_tiles,
+// column tile t % n_tiles), so the pairs running at one time share their A row tiles and B
+// through L2.  The producers stream every tile's K blocks through the ring without stopping
+// between tiles; the rank-0 MMA issuer accumulates tile i into TMEM accumulator i % 2 of both
+// CTAs; the epilogue warps drain accumulator i % 2 while the MMAs of tile i + 1 run in the other
+// one, and hand it back through the rank-0 CTA's tmem_empty barrier.
 template <bool BF16>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     cgemm_tcgen05_kernel(const __grid_constant__ CUtensorMap map_a0,
                          const __grid_constant__ CUtensorMap map_a1,
                          const __grid_constant__ CUtensorMap map_b0,
                          const __grid_constant__ CUtensorMap map_b1, GemmArgs args) {
+    using Cfg = GemmCfg<BF16>;
+    constexpr int S = Cfg::kStages;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-    uint64_t* empty = full + STAGES;
-    uint64_t* done = empty + STAGES;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Cfg::kStageBytes);  // rank 0's count
+    uint64_t* empty = full + S;            // per CTA, one multicast commit per round
+    uint64_t* tmem_full = empty + S;       // [2] per CTA: accumulator ready for the epilogue
+    uint64_t* tmem_empty = tmem_full + 2;  // [2] rank 0's count: drained by all 8 epilogue warps
+    uint64_t* done = tmem_empty + 2;       // per CTA: every MMA of the pair has finished
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
     int* issued_slot = reinterpret_cast<int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_tile = blockIdx.x, m_tile = blockIdx.y;
-    const int total = args.nseg * args.k_blocks;
+    const uint32_t rank = cluster_rank();  // 0 issues the MMAs of the pair
+    const int64_t first = blockIdx.x >> 1, stride = gridDim.x >> 1;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+        for (int i = 0; i < S; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&tmem_full[i], 1);
+            mbar_init(&tmem_empty[i], 8);  // 4 epilogue warps in each CTA
         }
         mbar_init(done, 1);
         *issued_slot = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+        // both CTAs' warp 1: the same 512 columns in each CTA's tensor memory
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
-                     "r"(TMEM_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+                     "r"(2 * TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
     }
     tc_fence_before();
     __syncthreads();
+    cluster_sync();  // both CTAs' barriers are initialised before any remote arrival
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
         if (lane == 0) {
-            const CUtensorMap* ma[2] = {&map_a0, &map_a1};
-            const CUtensorMap* mb[2] = {&map_b0, &map_b1};
-            int it = 0;
-            for (; it < total; ++it) {
-                const int s = it % STAGES;
-                const uint32_t ph = (it / STAGES) & 1u;
-                if (!mbar_wait(&empty[s], ph ^ 1u)) {
-                    atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_PRODUCER);
-                    break;
+            int it = 0;  // K blocks issued over all of this CTA's tiles
+            bool ok = true;
+            for (int64_t t = first; ok && t < args.tiles; t += stride) {
+                const int a_row = static_cast<int>(t / args.n_tiles) * BM + static_cast<int>(rank) * HALF;
+                const int b_row = static_cast<int>(t % args.n_tiles) * BN + static_cast<int>(rank) * HALF;
+                for (int kb = 0; kb < args.k_blocks; ++kb, ++it) {
+                    const int s = it % S;
+                    const uint32_t ph = (it / S) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u)) {
+                        atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_PRODUCER);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = smem + s * Cfg::kStageBytes;
+                    const uint32_t bar = cluster_addr(&full[s], 0);
+                    // rank 0 arms its barrier with the bytes of both CTAs' copies
+                    if (rank == 0) mbar_arrive_expect_tx(&full[s], 2 * Cfg::kStageBytes);
+                    const int k = kb * BK;
+                    tma_load_2d_pair(st, &map_a0, bar, k, a_row);
+                    if (BF16) tma_load_2d_pair(st + OP_TILE, &map_a1, bar, k, a_row);
+                    tma_load_2d_pair(st + Cfg::kPlanes * OP_TILE, &map_b0, bar, k, b_row);
+                    if (BF16) tma_load_2d_pair(st + 3 * OP_TILE, &map_b1, bar, k, b_row);
                 }
-                const int seg = it / args.k_blocks, kb = it % args.k_blocks;
-                uint8_t* sa = smem + s * STAGE_BYTES;
-                mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-                tma_load_2d(sa, ma[args.seg_a[seg]], &full[s], kb * BK, m_tile * BM);
-                tma_load_2d(sa + A_TILE, mb[args.seg_b[seg]], &full[s], kb * BK, n_tile * BN);
             }
             *issued_slot = it;
         }
     } else if (warp == 1) {
-        if (lane == 0) {
+        if (rank == 0 && lane == 0) {
             constexpr uint32_t idesc = mma_idesc(BF16);
             int it = 0;
-            for (; it < total; ++it) {
-                const int s = it % STAGES;
-                const uint32_t ph = (it / STAGES) & 1u;
-                if (!mbar_wait(&full[s], ph)) {
+            int i = 0;  // this pair's tile count
+            bool ok = true;
+            for (int64_t t = first; ok && t < args.tiles; t += stride, ++i) {
+                const int acc = i & 1;
+                const uint32_t use = static_cast<uint32_t>(i >> 1);
+                // the accumulator's previous tile must have been drained by both epilogues
+                if (!mbar_wait(&tmem_empty[acc], (use & 1u) ^ 1u)) {
                     atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_MMA);
                     break;
                 }
                 tc_fence_after();
-                const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
-                const uint64_t adesc = smem_desc_sw128(sa);
-                const uint64_t bdesc = smem_desc_sw128(sa + A_TILE);
+                const uint32_t d = tmem + static_cast<uint32_t>(acc * TMEM_COLS);
+                for (int kb = 0; kb < args.k_blocks; ++kb, ++it) {
+                    const int s = it % S;
+                    const uint32_t ph = (it / S) & 1u;
+                    if (!mbar_wait(&full[s], ph)) {
+                        atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_MMA);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(smem + s * Cfg::kStageBytes);
+                    const uint64_t a_hi = smem_desc_sw128(sa);
+                    const uint64_t b_hi = smem_desc_sw128(sa + Cfg::kPlanes * OP_TILE);
 #pragma unroll
-                for (int k = 0; k < BK / 16; ++k) {
-                    // K step of 16 elements = 32 bytes = 2 in the descriptor's address field
-                    mma_f16(tmem, adesc + 2u * k, bdesc + 2u * k, idesc, (it | k) != 0);
+                    for (int k = 0; k < BK / 16; ++k) {
+                        // K step of 16 elements = 32 bytes = 2 in the descriptor's address field
+                        mma_f16_pair(d, a_hi + 2u * k, b_hi + 2u * k, idesc, (kb | k) != 0);
+                        if (BF16) {
+                            const uint64_t a_lo = smem_desc_sw128(sa + OP_TILE);
+                            const uint64_t b_lo = smem_desc_sw128(sa + 3 * OP_TILE);
+                            mma_f16_pair(d, a_hi + 2u * k, b_lo + 2u * k, idesc, 1u);
+                            mma_f16_pair(d, a_lo + 2u * k, b_hi + 2u * k, idesc, 1u);
+                        }
+                    }
+                    mma_commit_pair(&empty[s]);  // stage s free in both CTAs once these finish
                 }
-                mma_commit(&empty[s]);
+                if (ok) mma_commit_pair(&tmem_full[acc]);  // the tile's accumulator is complete
             }
-            mma_commit(done);  // completes once every MMA issued above has finished
+            mma_commit_pair(done);  // completes once every MMA issued above has finished
         }
     } else {
-        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. rows of the tile
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, i.e. rows of this CTA's half tile
         const int q = warp & 3;
-        const int64_t row = static_cast<int64_t>(m_tile) * BM + q * 32 + lane;
-        // one lane waits, the warp follows converged (tcgen05.ld is warp-synchronous)
-        const int ok = __shfl_sync(0xffffffffu, lane == 0 ? (mbar_wait(done, 0) ? 1 : 0) : 0, 0);
-        __syncwarp();
-        if (!ok) {
-            atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_EPILOGUE);
-        } else {
+        const uint32_t drained0 = cluster_addr(&tmem_empty[0], 0);
+        const uint32_t drained1 = cluster_addr(&tmem_empty[1], 0);
+        int i = 0;
+        for (int64_t t = first; t < args.tiles; t += stride, ++i) {
+            const int acc = i & 1;
+            const uint32_t use = static_cast<uint32_t>(i >> 1);
+            const int n_tile = static_cast<int>(t % args.n_tiles);
+            const int64_t row = (t / args.n_tiles) * BM + static_cast<int64_t>(rank) * HALF + q * 32 + lane;
+            // one lane waits, the warp follows converged (tcgen05.ld is warp-synchronous)
+            const int ok = __shfl_sync(0xffffffffu,
+                                       lane == 0 ? (mbar_wait(&tmem_full[acc], use & 1u) ? 1 : 0) : 0, 0);
+            __syncwarp();
+            if (!ok) {
+                atomicCAS(args.err, ERR_NONE, ERR_TIMEOUT_EPILOGUE);
+                break;
+            }
             tc_fence_after();
             const float scale = (args.row_scale && row < args.m) ? args.row_scale[row] : 1.0f;
+            const uint32_t src = tmem + static_cast<uint32_t>(acc * TMEM_COLS) +
+                                 (static_cast<uint32_t>(q * 32) << 16);
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
                 uint32_t v[32];
-                tmem_ld_32cols(tmem + (static_cast<uint32_t>(q * 32) << 16) + c * 32, v);
+                tmem_ld_32cols(src + c * 32, v);
                 if (row < args.m) {
                     float4* dst = reinterpret_cast<float4*>(args.c + row * args.ldc +
                                                             static_cast<int64_t>(n_tile) * BN + c * 32);
 #pragma unroll
-                    for (int t = 0; t < 8; ++t) {
-                        dst[t] = make_float4(__uint_as_float(v[4 * t]) * scale,
-                                             __uint_as_float(v[4 * t + 1]) * scale,
-                                             __uint_as_float(v[4 * t + 2]) * scale,
-                                             __uint_as_float(v[4 * t + 3]) * scale);
+                    for (int u = 0; u < 8; ++u) {
+                        dst[u] = make_float4(__uint_as_float(v[4 * u]) * scale,
+                                             __uint_as_float(v[4 * u + 1]) * scale,
+                                             __uint_as_float(v[4 * u + 2]) * scale,
+                                             __uint_as_float(v[4 * u + 3]) * scale);
                     }
                 }
             }
+            // the accumulator may take the tile after next
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(acc ? drained1 : drained0);
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (threadIdx.x == 0 && *args.err != ERR_NONE) {
-        // drain: wait (bounded) for every stage this CTA's producer armed to land
-        const int issued = *issued_slot;
-        for (int it = (issued > STAGES ? issued - STAGES : 0); it < issued; ++it)
-            mbar_wait(&full[it % STAGES], (it / STAGES) & 1u);
-        mbar_wait(done, 0);
+    cluster_sync();  // both CTAs have issued everything and stopped waiting; errors are visible
+    if (threadIdx.x == 0) {
+        if (*static_cast<volatile unsigned*>(args.err) != ERR_NONE) {
+            // copies may still be in flight: rank 0 waits (bounded) for the last stages armed on
+            // its barriers, both CTAs then give any remaining copy time to land
+            if (rank == 0) {
+                const int issued = *issued_slot;
+                for (int it = (issued > S ? issued - S : 0); it < issued; ++it)
+                    mbar_wait(&full[it % S], (it / S) & 1u);
+            }
+            for (int i = 0; i < 1000; ++i) __nanosleep(1000);
+        }
+        mbar_wait(done, 0);  // no MMA may still write the tensor memory freed below
     }
     __syncthreads();
+    cluster_sync();
     if (warp == 1) {
         __syncwarp();
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(2 * TMEM_COLS));
     }
+    cluster_sync();  // neither CTA leaves while its peer still frees the pair's tensor memory
 }
 
 // ------------------------------------------------------------------ operand preparation
@@ -520,6 +645,45 @@ __global__ void copy_cols_kernel(const float* __restrict__ c, int64_t ldc, float
     out[i] = c[(i / cols) * ldc + (i % cols)];
 }
 
+// Co-resident CTA pairs of the GEMM kernel on a device (one CTA per SM by its shared memory),
+// cached per device and precision.
+constexpr int kPairCacheDevices = 64;
+std::atomic<int> g_gemm_pairs[kPairCacheDevices][2] = {};
+
+template <bool BF16>
+cudaError_t launch_gemm(const CUtensorMap& ma0, const CUtensorMap& ma1, const CUtensorMap& mb0,
+                        const CUtensorMap& mb1, const GemmArgs& a, int dev, cudaStream_t s) {
+    using Cfg = GemmCfg<BF16>;
+    auto* kern = cgemm_tcgen05_kernel<BF16>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Cfg::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(GEMM_THREADS);
+    cfg.dynamicSmemBytes = Cfg::kSmemBytes;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int pairs = (dev >= 0 && dev < kPairCacheDevices)
+                    ? g_gemm_pairs[dev][BF16 ? 1 : 0].load(std::memory_order_relaxed)
+                    : 0;
+    if (pairs <= 0) {
+        cfg.gridDim = dim3(2 * static_cast<unsigned>(num_sms() / 2));
+        if ((e = cudaOccupancyMaxActiveClusters(&pairs, kern, &cfg)) != cudaSuccess) return e;
+        if (pairs < 1) return cudaErrorInvalidConfiguration;
+        if (dev >= 0 && dev < kPairCacheDevices)
+            g_gemm_pairs[dev][BF16 ? 1 : 0].store(pairs, std::memory_order_relaxed);
+    }
+    const int64_t use = a.tiles < pairs ? a.tiles : pairs;
+    cfg.gridDim = dim3(2 * static_cast<unsigned>(use));
+    return cudaLaunchKernelEx(&cfg, kern, ma0, ma1, mb0, mb1, a);
+}
+
 }  // namespace mp
 }  // namespace afc
 
@@ -674,37 +838,28 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
         }
     }
     CUtensorMap ma0, ma1, mb0, mb1;
-    if ((e = make_map(&ma0, ws + L.a_hi, split, mm, L.kpad, BM)) != cudaSuccess ||
-        (e = make_map(&ma1, ws + (split ? L.a_lo : L.a_hi), split, mm, L.kpad, BM)) != cudaSuccess ||
-        (e = make_map(&mb0, ws + L.b_hi, split, L.npad, L.kpad, BN)) != cudaSuccess ||
-        (e = make_map(&mb1, ws + (split ? L.b_lo : L.b_hi), split, L.npad, L.kpad, BN)) != cudaSuccess) {
+    if ((e = make_map(&ma0, ws + L.a_hi, split, mm, L.kpad, HALF)) != cudaSuccess ||
+        (e = make_map(&ma1, ws + (split ? L.a_lo : L.a_hi), split, mm, L.kpad, HALF)) != cudaSuccess ||
+        (e = make_map(&mb0, ws + L.b_hi, split, L.npad, L.kpad, HALF)) != cudaSuccess ||
+        (e = make_map(&mb1, ws + (split ? L.b_lo : L.b_hi), split, L.npad, L.kpad, HALF)) != cudaSuccess) {
         set_error_message("AFC_MultiPatternApply: tensor map encoding failed");
         return AFC_ERR_CUDA;
     }
     GemmArgs a{};
     a.k_blocks = static_cast<int>(L.kpad / BK);
-    if (split) {
-        a.nseg = 3;  // hi*hi + hi*lo + lo*hi
-        a.seg_a[0] = 0; a.seg_b[0] = 0;
-        a.seg_a[1] = 0; a.seg_b[1] = 1;
-        a.seg_a[2] = 1; a.seg_b[2] = 0;
-    } else {
-        a.nseg = 1;
-        a.seg_a[0] = 0; a.seg_b[0] = 0;
-    }
     const bool direct = L.npad == 2 * K;
     a.c = direct ? d_out : reinterpret_cast<float*>(ws + L.c_pad);
     a.ldc = L.npad;
     a.m = mm;
     a.row_scale = split ? nullptr : reinterpret_cast<const float*>(ws + L.row_scale);
     a.err = err;
-    const dim3 grid(static_cast<unsigned>(L.npad / BN), static_cast<unsigned>((mm + BM - 1) / BM));
-    if (split) {
-        cudaFuncSetAttribute(cgemm_tcgen05_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        cgemm_tcgen05_kernel<true><<<grid, GEMM_THREADS, SMEM_BYTES, s>>>(ma0, ma1, mb0, mb1, a);
-    } else {
-        cudaFuncSetAttribute(cgemm_tcgen05_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        cgemm_tcgen05_kernel<false><<<grid, GEMM_THREADS, SMEM_BYTES, s>>>(ma0, ma1, mb0, mb1, a);
+    a.n_tiles = static_cast<int>(L.npad / BN);
+    a.tiles = static_cast<int64_t>(a.n_tiles) * ((mm + BM - 1) / BM);
+    e = split ? launch_gemm<true>(ma0, ma1, mb0, mb1, a, dev, s)
+              : launch_gemm<false>(ma0, ma1, mb0, mb1, a, dev, s);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return AFC_ERR_CUDA;
     }
     count_launch();
     if (!direct) {
