@@ -52,8 +52,11 @@ struct PointSet {
 cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const float* atten,
                                 int64_t n, PackedSource* out, cudaStream_t s);
 
+// The field of n packed sources at ps into out on stream s.  scratch_ok: a launch whose point
+// tiles would leave the last wave short may allocate partial sums (stream-ordered, from a
+// per-device pool) and cut the sources into chunks; otherwise it splits them over clusters.
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
-                         const PointSet& ps, void* out, cudaStream_t s);
+                         const PointSet& ps, void* out, cudaStream_t s, bool scratch_ok = true);
 
 // The rows tiling of a grid for `pairs` point pairs per thread (blocks of 1 << tx_log2
 // first-axis indices by (256 >> tx_log2) * 2 * pairs second-axis indices, one plane each), and

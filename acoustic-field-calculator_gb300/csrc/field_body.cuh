@@ -150,6 +150,16 @@ __device__ __forceinline__ void load_gtab(GTable& g) {
 // phases are first reduced to [-pi, pi] (ref_phase2).
 constexpr float kUnreducedPhaseMax = 640.0f;
 
+// Tiles whose phase bound lies above kUnreducedPhaseMax but at most kMidPhaseMax, with every
+// point in front of every source, take mid_phase2: r refined by a Newton step, phi fused,
+// reduced to [-pi, pi].  It stays within about an ulp of phi (6.1e-5 rad below 1,024 rad) of the
+// reference's rounding; larger phases take the reference's own rounding (ref_phase2).
+constexpr float kMidPhaseMax = 1024.0f;
+
+// Phase variants of the hot loops: unreduced (fast), Newton-refined and reduced (mid), or
+// rounded as the reference rounds it and reduced (ref).
+enum : int { kPhaseFast = 0, kPhaseMid = 1, kPhaseRef = 2 };
+
 // Neumaier's compensated addition: sum + v with the lost low-order part added to comp.
 __device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
     const float t = __fadd_rn(sum, v);
@@ -216,6 +226,19 @@ __device__ __forceinline__ float2 ref_phase2(float2 q2, float2 rinv, float2 k, f
     r = make_float2(refine_r(q2.x, rinv.x, q2.x * rinv.x), refine_r(q2.y, rinv.y, q2.y * rinv.y));
     const float2 ph = make_float2(__fadd_rn(phase.x, __fmul_rn(k.x, r.x)),
                                   __fadd_rn(phase.y, __fmul_rn(k.y, r.y)));
+    const float2 nq = add2(fma2(ph, f2(kInv2Pi), f2(kRoundMagic)), f2(-kRoundMagic));
+    return fma2(nq, f2(-kTwoPiLo), fma2(nq, f2(-kTwoPiHi), ph));
+}
+
+// The mid tiles' phase (kMidPhaseMax): r0 = r2 rinv (on entry in r) refined by one Newton step,
+// r = r0 + (r2 - r0^2) rinv / 2 (refine_r, packed), then phi = phase + k r with one rounding,
+// reduced to [-pi, pi] with 2 pi in two parts as ref_phase2 does.  The fused phi differs from
+// the reference's separately rounded product and sum by at most about an ulp of phi.
+__device__ __forceinline__ float2 mid_phase2(float2 r2, float2 rinv, float2 k, float2 phase,
+                                             float2& r) {
+    const float2 e = fma2(make_float2(-r.x, -r.y), r, r2);
+    r = fma2(e, mul2(rinv, f2(0.5f)), r);
+    const float2 ph = fma2(k, r, phase);
     const float2 nq = add2(fma2(ph, f2(kInv2Pi), f2(kRoundMagic)), f2(-kRoundMagic));
     return fma2(nq, f2(-kTwoPiLo), fma2(nq, f2(-kTwoPiHi), ph));
 }
@@ -288,12 +311,13 @@ struct PairGeom {
 // The PAIRS point pairs of one thread against shared-memory source j.  The hot loop only
 // records the smallest distance of any of the thread's points to the bin edge of its table
 // interval; that rare case recomputes the pairs' geometry to find which points, and corrects
-// them one by one.  RED: the careful variant, for tiles with a large phase bound or with some
-// point possibly behind a source: the phase is rounded as the reference rounds it and reduced
-// before sin/cos (ref_phase2, kUnreducedPhaseMax), and a cos(theta) next to -1 (kBackAxisC)
-// also takes the exact path.  The directivity comes straight from cos(theta), from the
+// them one by one.  PH: the phase variant.  kPhaseRef is the careful variant, for tiles with a
+// phase bound above kMidPhaseMax or with some point possibly behind a source: the phase is
+// rounded as the reference rounds it and reduced before sin/cos (ref_phase2), and a cos(theta)
+// next to -1 (kBackAxisC) also takes the exact path.  kPhaseMid: phases up to kMidPhaseMax,
+// every point in front (mid_phase2).  The directivity comes straight from cos(theta), from the
 // lane-replicated table (directivity2_gtab): no acos and no MUFU square root.
-template <int ST, int SUM, int PAIRS, bool UD, bool RED>
+template <int ST, int SUM, int PAIRS, bool UD, int PH>
 __device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTableLane& g, int j,
                                                   float3 n0, float2 (&PX)[PAIRS],
                                                   float2 (&PY)[PAIRS], float2 (&PZ)[PAIRS],
@@ -314,8 +338,10 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTab
         const PairGeom<UD> p(PX[q], PY[q], PZ[q], NP[q], v0, v1, v2, v3, ns);
         float2 r = mul2(p.r2, p.rinv);
         float2 red;
-        if constexpr (RED)
+        if constexpr (PH == kPhaseRef)
             red = ref_phase2(ref_dist2(p.dx, p.dy, p.dz), p.rinv, hi2(v1), hi2(v4), r);
+        else if constexpr (PH == kPhaseMid)
+            red = mid_phase2(p.r2, p.rinv, hi2(v1), hi2(v4), r);
         else red = fma2(hi2(v1), r, hi2(v4));
         const float2 ea = fma2(hi2(v3), r, lo2(v4));
         float2 w = mul2(p.rinv, make_float2(mufu_ex2(ea.x), mufu_ex2(ea.y)));
@@ -323,7 +349,7 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTab
             float2 t;
             w = mul2(w, directivity2_gtab(g, p.ct, t));
             near_min = fminf(near_min, fminf(fabsf(t.x), fabsf(t.y)));
-            if constexpr (RED) any_back |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
+            if constexpr (PH == kPhaseRef) any_back |= (p.ct.x < kBackAxisC) | (p.ct.y < kBackAxisC);
         }
         const float2 sn = make_float2(mufu_sin(red.x), mufu_sin(red.y));
         const float2 cs = make_float2(mufu_cos(red.x), mufu_cos(red.y));
@@ -355,6 +381,32 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTab
                 }
             }
         }
+    }
+}
+
+// Sources 0 .. cnt - 1 of the staged tile against the thread's points, with the tile's phase
+// variant.
+template <int ST, int SUM, int PAIRS, bool UD>
+__device__ __forceinline__ void source_loop(int ph, int cnt, const SmemTile& sm, const GTableLane& gl,
+                                            float3 n0, float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
+                                            float2 (&PZ)[PAIRS], float2 (&NP)[PAIRS],
+                                            float2 (&RE)[PAIRS], float2 (&IM)[PAIRS],
+                                            float2 (&CRE)[PAIRS], float2 (&CIM)[PAIRS]) {
+    if (ph == kPhaseFast) {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_source<ST, SUM, PAIRS, UD, kPhaseFast>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
+                                                              CRE, CIM);
+    } else if (ph == kPhaseMid) {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_source<ST, SUM, PAIRS, UD, kPhaseMid>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
+                                                             CRE, CIM);
+    } else {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_source<ST, SUM, PAIRS, UD, kPhaseRef>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
+                                                             CRE, CIM);
     }
 }
 
@@ -446,8 +498,9 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
         const int cnt = static_cast<int>((s_hi - t0) < kTile ? (s_hi - t0) : kTile);
         __syncthreads();
         // plain: every phase of the tile bounded for the unreduced path and every point in front
-        // of every source; otherwise the tile takes the careful variant (RED)
-        bool same_dir = true, plain = true;
+        // of every source; mid: the same with the phases within kMidPhaseMax; otherwise the
+        // tile takes the careful variant (kPhaseRef)
+        bool same_dir = true, plain = true, mid = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
             const PackedSource s = src[t0 + j];
             // |phi' + k r| over the box: r is at most the distance to the farthest corner
@@ -455,7 +508,9 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
             const float fy = fmaxf(fabsf(sm.bbox[1] - s.a.y), fabsf(sm.bbox[4] - s.a.y));
             const float fz = fmaxf(fabsf(sm.bbox[2] - s.a.z), fabsf(sm.bbox[5] - s.a.z));
             const float rmax = sqrtf(fmaf(fz, fz, fmaf(fy, fy, fx * fx)));
-            plain = plain && fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y)) <= kUnreducedPhaseMax;
+            const float bound = fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y));
+            plain = plain && bound <= kUnreducedPhaseMax;
+            mid = mid && bound <= kMidPhaseMax;
             if (ST == SRC_T4010A1) {
                 // the box's lowest n.(x - s) (per axis the corner n points away from): when it is
                 // not negative, every point is in front of the source, where cos(theta) >= 0
@@ -464,6 +519,7 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
                 const float lz = s.b.z >= 0.f ? sm.bbox[2] : sm.bbox[5];
                 const float front = fmaf(s.b.z, lz - s.a.z, fmaf(s.b.y, ly - s.a.y, s.b.x * (lx - s.a.x)));
                 plain = plain && front >= 0.f;
+                mid = mid && front >= 0.f;
             }
             sm.v0[j] = make_float4(-s.a.x, -s.a.x, -s.a.y, -s.a.y);
             sm.v1[j] = make_float4(-s.a.z, -s.a.z, s.a.w, s.a.w);
@@ -476,30 +532,12 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
         }
         const bool tile_same_dir = __syncthreads_and(same_dir);
         const bool tile_plain = __syncthreads_and(plain);
+        const bool tile_mid = __syncthreads_and(mid);
+        const int tile_ph = tile_plain ? kPhaseFast : (tile_mid ? kPhaseMid : kPhaseRef);
         if (ST == SRC_T4010A1 && tile_same_dir) {
-            if (tile_plain) {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, true, false>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
-                                                                   IM, CRE, CIM);
-            } else {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, true, true>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
-                                                                  CRE, CIM);
-            }
+            source_loop<ST, SUM, PAIRS, true>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
         } else {
-            if (tile_plain) {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, false, false>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
-                                                                    IM, CRE, CIM);
-            } else {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_source<ST, SUM, PAIRS, false, true>(sm, gl, j, n0, PX, PY, PZ, NP, RE,
-                                                                   IM, CRE, CIM);
-            }
+            source_loop<ST, SUM, PAIRS, false>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
         }
     }
 }

@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "afc_internal.h"
 #include "field_body.cuh"
@@ -156,6 +157,96 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (cg::this_cluster().block_rank() == 0)
         block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, GRID, g, pts, first, m, field,
                                 out);
+}
+
+// Work split of a chunked launch: `items` = tiles x chunks items in tile-major order (item
+// t * chunks + c: point tile t against source chunk c); block b of G takes the contiguous items
+// [start(b), start(b + 1)), `base` = items / G each and one more for the first `rem` blocks.
+struct ChunkSplit {
+    int64_t tiles, chunks, chunk;  // chunk: sources per chunk (the last one shorter)
+    int64_t base, rem;
+    // block that takes item i
+    __device__ __forceinline__ int64_t block_of(int64_t i) const {
+        const int64_t big = rem * (base + 1);
+        return i < big ? i / (base + 1) : rem + (i - big) / base;
+    }
+    __device__ __forceinline__ int64_t start(int64_t b) const {
+        return b * base + (b < rem ? b : rem);
+    }
+};
+
+// Persistent chunked launch of the general body for launches whose point tiles alone would
+// leave the last wave short.  A block's items of one tile are consecutive chunks, i.e. one
+// source range: a segment, summed by one block_accumulate pass.  A tile's segments are
+// numbered in chunk order (segment k of tile t begins where the k-th block after the tile's
+// first item's block begins), and segment k writes its sums at the tile's points to
+// partial[k * m + point]; field_chunk_combine_kernel adds them in that order.  The blocks'
+// loads differ by one chunk at most.  Each block fills its directivity tables once.
+template <int ST, bool GRID, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_chunk_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                       const float* __restrict__ pts, int64_t m, ChunkSplit cs,
+                       float2* __restrict__ partial) {
+    constexpr int kPPT = 2 * PAIRS;
+    __shared__ SmemTile sm;
+    GTable& gt = dynamic_gtab();
+    load_theta_table(sm, c_dir_table);
+    if constexpr (ST == SRC_T4010A1) load_gtab(gt);
+    const int64_t end = cs.start(blockIdx.x + 1);
+    for (int64_t it = cs.start(blockIdx.x); it < end;) {
+        const int64_t tile = it / cs.chunks;
+        const int64_t tile_end = (tile + 1) * cs.chunks;
+        const int64_t seg_end = end < tile_end ? end : tile_end;
+        const int64_t c0 = it - tile * cs.chunks, c1 = seg_end - tile * cs.chunks;
+        const int64_t lo = c0 * cs.chunk < n ? c0 * cs.chunk : n;
+        const int64_t hi = c1 * cs.chunk < n ? c1 * cs.chunk : n;
+        const int64_t k = cs.block_of(it) - cs.block_of(tile * cs.chunks);
+        const int64_t first = tile * (kThreads * kPPT);
+        float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+        block_accumulate<ST, SUM_PLAIN, PAIRS>(sm, gt, src, n, lo, hi, GRID, g, pts, m, first, RE,
+                                               IM, CRE, CIM);
+        float2* part = partial + k * m;
+#pragma unroll
+        for (int j = 0; j < kPPT; ++j) {
+            const int64_t q = first + threadIdx.x + static_cast<int64_t>(j) * kThreads;
+            if (q >= m) break;
+            part[q] = make_float2(lane_of(RE[j >> 1], j & 1), lane_of(IM[j >> 1], j & 1));
+        }
+        it = seg_end;
+    }
+}
+
+// The fields of a chunked launch: each point's segment sums added in segment order, the field
+// transform, and the coincident-source fix-up of the single-pass kernels for NaN sums.
+template <bool GRID>
+__global__ void __launch_bounds__(256)
+    field_chunk_combine_kernel(const float2* __restrict__ partial, ChunkSplit cs,
+                               int64_t tile_points, const PackedSource* __restrict__ src,
+                               int64_t n, GridDev g, const float* __restrict__ pts, int64_t m,
+                               int field, void* __restrict__ out) {
+    for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < m;
+         q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t t0 = (q / tile_points) * cs.chunks;
+        const int64_t segs = cs.block_of(t0 + cs.chunks - 1) - cs.block_of(t0) + 1;
+        float re = 0.f, im = 0.f;
+        for (int64_t k = 0; k < segs; ++k) {
+            const float2 v = partial[k * m + q];
+            re = __fadd_rn(re, v.x);
+            im = __fadd_rn(im, v.y);
+        }
+        store_field(out, q, field, re, im);
+        if (isnan(re) || isnan(im)) {
+            float x, y, z;
+            if (GRID) {
+                grid_point(g, q, x, y, z);
+            } else {
+                x = pts[3 * q];
+                y = pts[3 * q + 1];
+                z = pts[3 * q + 2];
+            }
+            fix_coincident(src, n, x, y, z, q, field, out);
+        }
+    }
 }
 
 // Mid-size grids: the rows tiling with every tile's sources split over a cluster of S blocks,
@@ -285,19 +376,187 @@ int64_t split_width(int64_t blocks, int64_t n, Slots slots) {
     return best;
 }
 
+// Chunked launches (field_chunk_kernel): chunks of kChunkSources sources (one: the blocks'
+// loads differ by one source iteration at most; a block's consecutive chunks of a tile are one
+// pass whatever their size), partial sums of at most kChunkMaxBytes.
+constexpr int64_t kChunkSources = 1;
+constexpr int64_t kChunkMaxBytes = 256LL << 20;
+
+// Modelled time of the general body's launch options over `tiles` point tiles of n sources
+// each, in source iterations of one block (about 0.67 us at 4 point pairs per thread on a
+// GB300).  Calibrated on 3,984 sources and 65,536 to 4,194,304
+// scatter points: an item of 2,048 points and 210 sources took 148.5 us against 140.6 us of
+// source iterations, so the set-up of a pass over a source range (its points, their bounding
+// box, the partial staging tile, the store) costs about 11 iterations, and a chunked launch
+// about 20 us more than its passes (the combine launch, the drain).
+// Its source iterations ran 2.5 % slower than the single-pass kernel's at full waves (4,194,304
+// points: 0.688 against 0.671 us), so it is taken only where the single pass and the cluster
+// split leave their last wave less than 90 % full, and only at 4 point pairs per thread, where
+// it was calibrated.
+constexpr double kPassSetup = 11.0;
+constexpr double kChunkFixedUs = 20.0;
+constexpr double kChunkIterationUs = 0.688;
+constexpr double kChunkSlowdown = 1.025;
+constexpr double kChunkBelowFill = 0.9;
+
+// fraction of `slots` resident blocks that `blocks` blocks keep busy over their waves
+double wave_fill(int64_t blocks, int64_t slots) {
+    const int64_t waves = (blocks + slots - 1) / slots;
+    return waves > 0 ? static_cast<double>(blocks) / static_cast<double>(waves * slots) : 1.0;
+}
+
+// one pass per tile (field_direct_kernel) on `slots` resident blocks
+double direct_cost(int64_t tiles, int64_t n, int64_t slots) {
+    const int64_t waves = (tiles + slots - 1) / slots;
+    return static_cast<double>(waves) * (static_cast<double>(n) + kPassSetup);
+}
+
+// S blocks per tile in clusters (field_split_kernel) on `slots` resident blocks of S-clusters
+double split_cost(int64_t tiles, int64_t n, int64_t S, int64_t slots) {
+    const int64_t waves = (tiles * S + slots - 1) / slots;
+    return static_cast<double>(waves) *
+           (static_cast<double>((n + S - 1) / S) + kPassSetup + 2.0);
+}
+
+// the chunked launch on `blocks` persistent blocks: the largest block's chunks, up to two
+// passes, the fixed cost, at the chunked kernel's iteration rate
+double chunk_cost(int64_t tiles, int64_t n, int64_t blocks) {
+    const int64_t chunks = (n + kChunkSources - 1) / kChunkSources;
+    const int64_t per = (tiles * chunks + blocks - 1) / blocks;
+    return kChunkSlowdown * (static_cast<double>(per * kChunkSources) + 2.0 * kPassSetup) +
+           kChunkFixedUs / kChunkIterationUs;
+}
+
+// The work split of a chunked launch of `tiles` tiles and n sources on `blocks` blocks, and the
+// partial-sum slots it needs per point (the most segments any tile has).
+ChunkSplit chunk_split(int64_t tiles, int64_t n, int64_t blocks, int64_t* slots_per_point) {
+    ChunkSplit cs{};
+    cs.tiles = tiles;
+    cs.chunks = (n + kChunkSources - 1) / kChunkSources;
+    cs.chunk = kChunkSources;
+    const int64_t items = tiles * cs.chunks;
+    if (blocks > items) blocks = items;
+    cs.base = items / blocks;
+    cs.rem = items % blocks;
+    // a tile's chunks - 1 item boundaries after its first item start at most
+    // ceil((chunks - 1) / base) more blocks
+    *slots_per_point = cs.base > 0 ? (cs.chunks - 1 + cs.base - 1) / cs.base + 1 : cs.chunks;
+    return cs;
+}
+
+// Per-device pool of the chunked launches' partial sums: stream-ordered allocations that keep
+// up to kChunkMaxBytes after they are freed, so that repeated calls do not return memory to the
+// driver and take it again.
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kSmCacheDevices] = {};
+
+cudaError_t scratch_alloc(void** ptr, size_t bytes, cudaStream_t s) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kSmCacheDevices) return cudaErrorMemoryAllocation;
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mu);
+        if (!g_pools[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+            uint64_t keep = static_cast<uint64_t>(kChunkMaxBytes);
+            if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) !=
+                cudaSuccess) {
+                cudaMemPoolDestroy(pool);
+                return e;
+            }
+            g_pools[dev] = pool;
+        }
+        pool = g_pools[dev];
+    }
+    return cudaMallocFromPoolAsync(ptr, bytes, pool, s);
+}
+
 // Dynamic shared memory of a general-body kernel for source type ST.
 template <int ST>
 constexpr int gtab_bytes() {
     return ST == SRC_T4010A1 ? kGTableBytes : 0;
 }
 
+// A chunked launch of the general body (field_chunk_kernel + field_chunk_combine_kernel) on
+// `blocks` persistent blocks.  cudaErrorMemoryAllocation: no scratch for the partial sums
+// (nothing was launched).
+template <int ST, bool GRID, int PAIRS>
+cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& ps, int field,
+                           void* out, cudaStream_t s, int64_t tiles, int64_t blocks) {
+    constexpr int kDyn = gtab_bytes<ST>();
+    int64_t slots = 0;
+    const ChunkSplit cs = chunk_split(tiles, n, blocks, &slots);
+    const size_t bytes = sizeof(float2) * static_cast<size_t>(slots) * static_cast<size_t>(ps.m);
+    if (static_cast<int64_t>(bytes) > kChunkMaxBytes) return cudaErrorMemoryAllocation;
+    void* partial = nullptr;
+    if (scratch_alloc(&partial, bytes, s) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cudaErrorMemoryAllocation;
+    }
+    cudaError_t e = allow_dynamic_smem<field_chunk_kernel<ST, GRID, PAIRS>>(kDyn);
+    if (e == cudaSuccess) {
+        const int64_t items = tiles * cs.chunks;
+        field_chunk_kernel<ST, GRID, PAIRS><<<static_cast<unsigned>(blocks < items ? blocks : items), kThreads, kDyn, s>>>(
+            src, n, ps.grid, ps.pts, ps.m, cs, static_cast<float2*>(partial));
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        const int64_t want = (ps.m + 255) / 256, cap = 8LL * num_sms();
+        field_chunk_combine_kernel<GRID><<<static_cast<unsigned>(want < cap ? want : cap), 256, 0, s>>>(
+            static_cast<const float2*>(partial), cs, static_cast<int64_t>(kThreads) * 2 * PAIRS,
+            src, n, ps.grid, ps.pts, ps.m, field, out);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    const cudaError_t ef = cudaFreeAsync(partial, s);
+    return e != cudaSuccess ? e : ef;
+}
+
 template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
-                         void* out, cudaStream_t s) {
+                         void* out, cudaStream_t s, bool scratch_ok) {
     constexpr int kDyn = gtab_bytes<ST>();
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
+    if (PAIRS == 4 && !rows.use && SUM == SUM_PLAIN && scratch_ok && n >= 2 * kChunkSources) {
+        // chunked (not while the stream is being captured: the partial sums are allocated on
+        // the stream) when the single pass and the cluster split leave their last wave short and
+        // the model puts it below both
+        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cst) == cudaSuccess && cst == cudaStreamCaptureStatusNone) {
+            const int64_t slots1 = resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn);
+            double other = direct_cost(flat_blocks, n, slots1);
+            double other_fill = wave_fill(flat_blocks, slots1);
+            for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
+                const int64_t slots = resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(S, kDyn);
+                const double c = split_cost(flat_blocks, n, S, slots);
+                if (c < other) {
+                    other = c;
+                    other_fill = wave_fill(flat_blocks * S, slots);
+                }
+            }
+            const int64_t blocks =
+                ps.is_grid ? resident_blocks<field_chunk_kernel<ST, true, PAIRS>>(1, kDyn)
+                           : resident_blocks<field_chunk_kernel<ST, false, PAIRS>>(1, kDyn);
+            if (other_fill < kChunkBelowFill && chunk_cost(flat_blocks, n, blocks) < other) {
+                const cudaError_t e =
+                    ps.is_grid ? launch_chunked<ST, true, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks)
+                               : launch_chunked<ST, false, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks);
+                if (e != cudaErrorMemoryAllocation) return e;
+            }
+        } else {
+            (void)cudaGetLastError();
+        }
+    }
     if (!rows.use) {
         // flat numbering whose blocks would leave the last wave short (or the GPU part empty):
         // split each tile's sources over a cluster
@@ -395,15 +654,15 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
 // few even split 8 ways).
 template <int ST>
 cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
-                      int field, void* out, cudaStream_t s) {
+                      int field, void* out, cudaStream_t s, bool scratch_ok) {
     if (sum_mode == SUM_COMPENSATED)
-        return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s);
+        return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s, false);
     const bool rows_grid = ps.is_grid && ps.grid.count[1] > 1;  // the rows body can take it
     const int64_t four_from = rows_grid ? 131072 : 32768;
     const int64_t two_from = rows_grid ? 32768 : INT64_MAX;
-    if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s);
-    if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s);
-    return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s);
+    if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s, scratch_ok);
+    if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s, scratch_ok);
+    return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s, scratch_ok);
 }
 
 }  // namespace
@@ -452,11 +711,11 @@ cudaError_t launch_pack_sources(int st, const float* raw, const float* k, const 
 }
 
 cudaError_t launch_field(int st, int field, int sum_mode, const PackedSource* src, int64_t n,
-                         const PointSet& ps, void* out, cudaStream_t s) {
+                         const PointSet& ps, void* out, cudaStream_t s, bool scratch_ok) {
     if (ps.m <= 0) return cudaSuccess;
     if (field < FIELD_PRESSURE || field > FIELD_COMPLEX) return cudaErrorInvalidValue;
-    if (st == SRC_T4010A1) return launch_st<SRC_T4010A1>(sum_mode, src, n, ps, field, out, s);
-    if (st == SRC_SPHERE) return launch_st<SRC_SPHERE>(sum_mode, src, n, ps, field, out, s);
+    if (st == SRC_T4010A1) return launch_st<SRC_T4010A1>(sum_mode, src, n, ps, field, out, s, scratch_ok);
+    if (st == SRC_SPHERE) return launch_st<SRC_SPHERE>(sum_mode, src, n, ps, field, out, s, scratch_ok);
     return cudaErrorInvalidValue;
 }
 

@@ -108,7 +108,9 @@ extern "C" int32_t AFC_FieldGridDeviceNoAlloc(int32_t source_type, int32_t field
                                 static_cast<int64_t>(n), packed, s);
         if (e != cudaSuccess) return fail(AFC_ERR_CUDA, cudaGetErrorString(e));
     }
-    e = launch_field(source_type, field_type, sum_mode, packed, static_cast<int64_t>(n), ps, d_out, s);
+    // no partial-sum scratch: this entry point allocates nothing
+    e = launch_field(source_type, field_type, sum_mode, packed, static_cast<int64_t>(n), ps, d_out, s,
+                     false);
     if (e != cudaSuccess) return fail(AFC_ERR_CUDA, cudaGetErrorString(e));
     return AFC_OK;
 }

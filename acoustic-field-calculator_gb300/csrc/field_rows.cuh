@@ -108,7 +108,7 @@ static __device__ __noinline__ float2 edge_correction_rows(const float4* __restr
 // n_a1), v3 = (n_a2, n_a2, a2, a2)).  p0, p2: the thread's coordinates along the first and
 // third grid axes; U: its points' coordinates along the second; n0a: the shared direction (of
 // source 0) in grid axis order, which every source of a UD tile has.
-template <int ST, int SUM, int PAIRS, bool UD, bool RED>
+template <int ST, int SUM, int PAIRS, bool UD, int PH>
 __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, const RowsTable& rt, int j,
                                                 float p0, float p2,
                                                 int a0, int a1, float3 n0a, float2 (&U)[PAIRS],
@@ -129,18 +129,20 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, const RowsTa
     sh.nvw = 0.f;
     if constexpr (ST == SRC_T4010A1 && !UD) sh.nvw = fmaf(v3.x, sh.dw, v2.x * sh.dv);
     sh.qb = sh.qc = 0.f;
-    if constexpr (RED) row_q2_parts(sh.dv, sh.dw, a0, a1, sh.qb, sh.qc);
+    if constexpr (PH == kPhaseRef) row_q2_parts(sh.dv, sh.dw, a0, a1, sh.qb, sh.qc);
     float near_min = kCTabMargin;  // smallest |c - L| of the thread's points (the edge test)
 #pragma unroll
     for (int q = 0; q < PAIRS; ++q) {
         const RowGeom<UD> p(U[q], NP[q], sh, v0, v2, ns);
         float2 r = mul2(p.r2, p.rinv);
         float2 red;
-        if constexpr (RED) {
+        if constexpr (PH == kPhaseRef) {
             const float2 q2 =
                 make_float2(__fadd_rn(__fadd_rn(__fmul_rn(p.du.x, p.du.x), sh.qb), sh.qc),
                             __fadd_rn(__fadd_rn(__fmul_rn(p.du.y, p.du.y), sh.qb), sh.qc));
             red = ref_phase2(q2, p.rinv, hi2(v1), hi2(v4), r);
+        } else if constexpr (PH == kPhaseMid) {
+            red = mid_phase2(p.r2, p.rinv, hi2(v1), hi2(v4), r);
         } else {
             red = fma2(hi2(v1), r, hi2(v4));
         }
@@ -189,6 +191,33 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, const RowsTa
                 }
             }
         }
+    }
+}
+
+// Sources 0 .. cnt - 1 of the staged tile against the thread's points (accumulate_rows), with
+// the tile's phase variant.
+template <int ST, int SUM, int PAIRS, bool UD>
+__device__ __forceinline__ void rows_source_loop(int ph, int cnt, const SmemTile& sm,
+                                                 const RowsTable& rt, float p0, float p2, int a0,
+                                                 int a1, float3 n0a, float2 (&U)[PAIRS],
+                                                 float2 (&NP)[PAIRS], float2 (&RE)[PAIRS],
+                                                 float2 (&IM)[PAIRS], float2 (&CRE)[PAIRS],
+                                                 float2 (&CIM)[PAIRS]) {
+    if (ph == kPhaseFast) {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_rows<ST, SUM, PAIRS, UD, kPhaseFast>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
+                                                            RE, IM, CRE, CIM);
+    } else if (ph == kPhaseMid) {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_rows<ST, SUM, PAIRS, UD, kPhaseMid>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
+                                                           RE, IM, CRE, CIM);
+    } else {
+#pragma unroll 1
+        for (int j = 0; j < cnt; ++j)
+            accumulate_rows<ST, SUM, PAIRS, UD, kPhaseRef>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
+                                                           RE, IM, CRE, CIM);
     }
 }
 
@@ -289,14 +318,16 @@ __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const RowsTable& r
     for (int64_t s0 = s_lo; s0 < s_hi; s0 += kTile) {
         const int cnt = static_cast<int>((s_hi - s0) < kTile ? (s_hi - s0) : kTile);
         __syncthreads();
-        bool same_dir = true, small_phase = true;
+        bool same_dir = true, small_phase = true, mid_phase = true;
         for (int j = threadIdx.x; j < cnt; j += kThreads) {
             const PackedSource s = src[s0 + j];
             const float fx = fmaxf(fabsf(sm.bbox[0] - s.a.x), fabsf(sm.bbox[3] - s.a.x));
             const float fy = fmaxf(fabsf(sm.bbox[1] - s.a.y), fabsf(sm.bbox[4] - s.a.y));
             const float fz = fmaxf(fabsf(sm.bbox[2] - s.a.z), fabsf(sm.bbox[5] - s.a.z));
             const float rmax = sqrtf(fmaf(fz, fz, fmaf(fy, fy, fx * fx)));
-            small_phase = small_phase && fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y)) <= kUnreducedPhaseMax;
+            const float bound = fmaf(fabsf(s.a.w), rmax, fabsf(s.c.y));
+            small_phase = small_phase && bound <= kUnreducedPhaseMax;
+            mid_phase = mid_phase && bound <= kMidPhaseMax;
             const float s0_ = pick3(s.a.x, s.a.y, s.a.z, a0), s1_ = pick3(s.a.x, s.a.y, s.a.z, a1),
                         s2_ = pick3(s.a.x, s.a.y, s.a.z, a2);
             const float m0 = pick3(s.b.x, s.b.y, s.b.z, a0), m1 = pick3(s.b.x, s.b.y, s.b.z, a1),
@@ -312,31 +343,14 @@ __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const RowsTable& r
         }
         const bool tile_same_dir = __syncthreads_and(same_dir);
         const bool tile_small = __syncthreads_and(small_phase);
-        if (ST == SRC_T4010A1 && tile_same_dir) {
-            if (tile_small) {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, true, false>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
-                                                                 IM, CRE, CIM);
-            } else {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, true, true>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
-                                                                IM, CRE, CIM);
-            }
-        } else {
-            if (tile_small) {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, false, false>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
-                                                                  RE, IM, CRE, CIM);
-            } else {
-#pragma unroll 1
-                for (int j = 0; j < cnt; ++j)
-                    accumulate_rows<ST, SUM, PAIRS, false, true>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP, RE,
-                                                                 IM, CRE, CIM);
-            }
-        }
+        const bool tile_mid = __syncthreads_and(mid_phase);
+        const int tile_ph = tile_small ? kPhaseFast : (tile_mid ? kPhaseMid : kPhaseRef);
+        if (ST == SRC_T4010A1 && tile_same_dir)
+            rows_source_loop<ST, SUM, PAIRS, true>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U, NP,
+                                                   RE, IM, CRE, CIM);
+        else
+            rows_source_loop<ST, SUM, PAIRS, false>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U, NP,
+                                                    RE, IM, CRE, CIM);
     }
 
 }

@@ -337,7 +337,8 @@ class Engine {
                 return e;
             PointSet ps = r.ps;
             if (!ps.is_grid) ps.pts = reinterpret_cast<const float*>(d + L.pts);
-            if ((e = launch_field(g.st, r.field, SUM_PLAIN, packed, n, ps, d + L.out, s)) != cudaSuccess)
+            // device memory only from the engine's budgeted arena: no partial-sum scratch
+            if ((e = launch_field(g.st, r.field, SUM_PLAIN, packed, n, ps, d + L.out, s, false)) != cudaSuccess)
                 return e;
             if (r.out_bytes &&
                 (e = cudaMemcpyAsync(h + r.h_out, d + L.out, r.out_bytes, cudaMemcpyDeviceToHost, s)) !=
@@ -363,7 +364,7 @@ class Engine {
             auto* packed = reinterpret_cast<PackedSource*>(d + o_pk);
             if ((e = launch_repack(g.d_packed, nullptr, nullptr, ap, n, packed, s)) != cudaSuccess)
                 return e;
-            if ((e = launch_field(g.st, FIELD_PRESSURE, SUM_PLAIN, packed, n, r.ps, d + o_out, s)) !=
+            if ((e = launch_field(g.st, FIELD_PRESSURE, SUM_PLAIN, packed, n, r.ps, d + o_out, s, false)) !=
                 cudaSuccess)
                 return e;
             if (r.out_bytes &&
