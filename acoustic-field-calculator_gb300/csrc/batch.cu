@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const Item w = items[it];
         const JobDev J = jobs[w.job];
         const JobTile T = tiles[w.job];
-        block_rows<ST, SUM_PLAIN, PAIRS>(sm, rt, arena + J.src_off, J.n, J.g, T.tx_log2,
+        block_rows<ST, SUM_PLAIN, PAIRS, true>(sm, rt, arena + J.src_off, J.n, J.g, T.tx_log2,
                                          T.tiles0, T.tiles1, w.block, J.field, J.out);
     }
 }
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const Item w = items[it];
         const JobDev J = jobs[w.job];
         const int64_t first = static_cast<int64_t>(w.block) * (kThreads * 2 * PAIRS);
-        block_points<ST, SUM_PLAIN, PAIRS>(sm, gt, arena + J.src_off, J.n, J.is_grid != 0, J.g,
+        block_points<ST, SUM_PLAIN, PAIRS, true>(sm, gt, arena + J.src_off, J.n, J.is_grid != 0, J.g,
                                            J.pts, J.m, first, J.field, J.out);
     }
 }

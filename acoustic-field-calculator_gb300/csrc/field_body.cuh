@@ -385,8 +385,9 @@ __device__ __forceinline__ void accumulate_source(const SmemTile& sm, const GTab
 }
 
 // Sources 0 .. cnt - 1 of the staged tile against the thread's points, with the tile's phase
-// variant.
-template <int ST, int SUM, int PAIRS, bool UD>
+// variant (MID: whether the mid tier is compiled in; without it, mid tiles take the careful
+// variant).
+template <int ST, int SUM, int PAIRS, bool UD, bool MID>
 __device__ __forceinline__ void source_loop(int ph, int cnt, const SmemTile& sm, const GTableLane& gl,
                                             float3 n0, float2 (&PX)[PAIRS], float2 (&PY)[PAIRS],
                                             float2 (&PZ)[PAIRS], float2 (&NP)[PAIRS],
@@ -397,7 +398,7 @@ __device__ __forceinline__ void source_loop(int ph, int cnt, const SmemTile& sm,
         for (int j = 0; j < cnt; ++j)
             accumulate_source<ST, SUM, PAIRS, UD, kPhaseFast>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
                                                               CRE, CIM);
-    } else if (ph == kPhaseMid) {
+    } else if (MID && ph == kPhaseMid) {
 #pragma unroll 1
         for (int j = 0; j < cnt; ++j)
             accumulate_source<ST, SUM, PAIRS, UD, kPhaseMid>(sm, gl, j, n0, PX, PY, PZ, NP, RE, IM,
@@ -414,7 +415,7 @@ __device__ __forceinline__ void source_loop(int ph, int cnt, const SmemTile& sm,
 // s_lo .. s_hi - 1 tile by tile into `sm` (its dir table must already be filled) and accumulate
 // their fields into RE, IM (CRE, CIM: compensation terms).  `grid` selects generated grid
 // points or explicit ones; source 0's direction is the shared direction of the fast cos(theta).
-template <int ST, int SUM, int PAIRS>
+template <int ST, int SUM, int PAIRS, bool MID = false>
 __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
                                                  const PackedSource* __restrict__ src,
                                                  int64_t n, int64_t s_lo, int64_t s_hi, bool grid,
@@ -533,11 +534,11 @@ __device__ __forceinline__ void block_accumulate(SmemTile& sm, const GTable& gt,
         const bool tile_same_dir = __syncthreads_and(same_dir);
         const bool tile_plain = __syncthreads_and(plain);
         const bool tile_mid = __syncthreads_and(mid);
-        const int tile_ph = tile_plain ? kPhaseFast : (tile_mid ? kPhaseMid : kPhaseRef);
+        const int tile_ph = tile_plain ? kPhaseFast : ((MID && tile_mid) ? kPhaseMid : kPhaseRef);
         if (ST == SRC_T4010A1 && tile_same_dir) {
-            source_loop<ST, SUM, PAIRS, true>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+            source_loop<ST, SUM, PAIRS, true, MID>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
         } else {
-            source_loop<ST, SUM, PAIRS, false>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
+            source_loop<ST, SUM, PAIRS, false, MID>(tile_ph, cnt, sm, gl, n0, PX, PY, PZ, NP, RE, IM, CRE, CIM);
         }
     }
 }
@@ -633,14 +634,14 @@ __device__ __forceinline__ void block_store(float2 (&RE)[PAIRS], float2 (&IM)[PA
 
 // One block of 2*PAIRS*kThreads observation points starting at point `first`, all n sources:
 // accumulate, apply the field transform and store.
-template <int ST, int SUM, int PAIRS>
+template <int ST, int SUM, int PAIRS, bool MID = false>
 __device__ __forceinline__ void block_points(SmemTile& sm, const GTable& gt,
                                              const PackedSource* __restrict__ src, int64_t n,
                                              bool grid, const GridDev& g,
                                              const float* __restrict__ pts, int64_t m,
                                              int64_t first, int field, void* __restrict__ out) {
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    block_accumulate<ST, SUM, PAIRS>(sm, gt, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE,
+    block_accumulate<ST, SUM, PAIRS, MID>(sm, gt, src, n, 0, n, grid, g, pts, m, first, RE, IM, CRE,
                                      CIM);
     block_store<SUM, PAIRS>(RE, IM, CRE, CIM, src, n, grid, g, pts, first, m, field, out);
 }

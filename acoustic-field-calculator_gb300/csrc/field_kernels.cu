@@ -390,19 +390,22 @@ constexpr int64_t kChunkMaxBytes = 256LL << 20;
 // box, the partial staging tile, the store) costs about 11 iterations, and a chunked launch
 // about 20 us more than its passes (the combine launch, the drain).
 // Its source iterations ran 2.5 % slower than the single-pass kernel's at full waves (4,194,304
-// points: 0.688 against 0.671 us), so it is taken only where the single pass and the cluster
-// split leave their last wave less than 90 % full, and only at 4 point pairs per thread, where
-// it was calibrated.
+// points: 0.688 against 0.671 us).  A launch of several waves loses less to a short last wave
+// than the wave count says (the blocks of that wave share their SMs with fewer others and run
+// faster), so the chunked launch does not replace one of two or more waves that fills at least
+// 90 % of its slots; it is taken only at 4 point pairs per thread, where it was calibrated.
 constexpr double kPassSetup = 11.0;
 constexpr double kChunkFixedUs = 20.0;
 constexpr double kChunkIterationUs = 0.688;
 constexpr double kChunkSlowdown = 1.025;
 constexpr double kChunkBelowFill = 0.9;
 
-// fraction of `slots` resident blocks that `blocks` blocks keep busy over their waves
-double wave_fill(int64_t blocks, int64_t slots) {
+// whether `blocks` blocks on `slots` resident ones run two or more waves that keep at least
+// kChunkBelowFill of the slots busy
+bool full_waves(int64_t blocks, int64_t slots) {
     const int64_t waves = (blocks + slots - 1) / slots;
-    return waves > 0 ? static_cast<double>(blocks) / static_cast<double>(waves * slots) : 1.0;
+    return waves >= 2 && static_cast<double>(blocks) >=
+                             kChunkBelowFill * static_cast<double>(waves * slots);
 }
 
 // one pass per tile (field_direct_kernel) on `slots` resident blocks
@@ -529,25 +532,25 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
     if (PAIRS == 4 && !rows.use && SUM == SUM_PLAIN && scratch_ok && n >= 2 * kChunkSources) {
         // chunked (not while the stream is being captured: the partial sums are allocated on
-        // the stream) when the single pass and the cluster split leave their last wave short and
-        // the model puts it below both
+        // the stream) when the model puts it below the single pass and the cluster split and
+        // neither runs full waves
         cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(s, &cst) == cudaSuccess && cst == cudaStreamCaptureStatusNone) {
             const int64_t slots1 = resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn);
             double other = direct_cost(flat_blocks, n, slots1);
-            double other_fill = wave_fill(flat_blocks, slots1);
+            bool other_full = full_waves(flat_blocks, slots1);
             for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
                 const int64_t slots = resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(S, kDyn);
                 const double c = split_cost(flat_blocks, n, S, slots);
                 if (c < other) {
                     other = c;
-                    other_fill = wave_fill(flat_blocks * S, slots);
+                    other_full = full_waves(flat_blocks * S, slots);
                 }
             }
             const int64_t blocks =
                 ps.is_grid ? resident_blocks<field_chunk_kernel<ST, true, PAIRS>>(1, kDyn)
                            : resident_blocks<field_chunk_kernel<ST, false, PAIRS>>(1, kDyn);
-            if (other_fill < kChunkBelowFill && chunk_cost(flat_blocks, n, blocks) < other) {
+            if (!other_full && chunk_cost(flat_blocks, n, blocks) < other) {
                 const cudaError_t e =
                     ps.is_grid ? launch_chunked<ST, true, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks)
                                : launch_chunked<ST, false, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks);

@@ -195,8 +195,9 @@ __device__ __forceinline__ void accumulate_rows(const SmemTile& sm, const RowsTa
 }
 
 // Sources 0 .. cnt - 1 of the staged tile against the thread's points (accumulate_rows), with
-// the tile's phase variant.
-template <int ST, int SUM, int PAIRS, bool UD>
+// the tile's phase variant (MID: whether the mid tier is compiled in; without it, mid tiles take
+// the careful variant).
+template <int ST, int SUM, int PAIRS, bool UD, bool MID>
 __device__ __forceinline__ void rows_source_loop(int ph, int cnt, const SmemTile& sm,
                                                  const RowsTable& rt, float p0, float p2, int a0,
                                                  int a1, float3 n0a, float2 (&U)[PAIRS],
@@ -208,7 +209,7 @@ __device__ __forceinline__ void rows_source_loop(int ph, int cnt, const SmemTile
         for (int j = 0; j < cnt; ++j)
             accumulate_rows<ST, SUM, PAIRS, UD, kPhaseFast>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
                                                             RE, IM, CRE, CIM);
-    } else if (ph == kPhaseMid) {
+    } else if (MID && ph == kPhaseMid) {
 #pragma unroll 1
         for (int j = 0; j < cnt; ++j)
             accumulate_rows<ST, SUM, PAIRS, UD, kPhaseMid>(sm, rt, j, p0, p2, a0, a1, n0a, U, NP,
@@ -231,7 +232,7 @@ __device__ __forceinline__ float axis_coord(const GridDev& g, int k, int a, int6
 // One tile of the rows tiling (tile index -> (t0, t1) of plane i2; TX = 1 << tx_log2): the sums
 // of sources s_lo .. s_hi - 1 at the thread's points, in RE, IM (CRE, CIM: compensations).
 // Source 0's direction is the shared direction of the fast cos(theta) whatever the range.
-template <int ST, int SUM, int PAIRS>
+template <int ST, int SUM, int PAIRS, bool MID = false>
 __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const RowsTable& rt,
                                                 const PackedSource* __restrict__ src,
                                                 int64_t n, int64_t s_lo, int64_t s_hi,
@@ -344,13 +345,13 @@ __device__ __forceinline__ void rows_accumulate(SmemTile& sm, const RowsTable& r
         const bool tile_same_dir = __syncthreads_and(same_dir);
         const bool tile_small = __syncthreads_and(small_phase);
         const bool tile_mid = __syncthreads_and(mid_phase);
-        const int tile_ph = tile_small ? kPhaseFast : (tile_mid ? kPhaseMid : kPhaseRef);
+        const int tile_ph = tile_small ? kPhaseFast : ((MID && tile_mid) ? kPhaseMid : kPhaseRef);
         if (ST == SRC_T4010A1 && tile_same_dir)
-            rows_source_loop<ST, SUM, PAIRS, true>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U, NP,
-                                                   RE, IM, CRE, CIM);
+            rows_source_loop<ST, SUM, PAIRS, true, MID>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U,
+                                                        NP, RE, IM, CRE, CIM);
         else
-            rows_source_loop<ST, SUM, PAIRS, false>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U, NP,
-                                                    RE, IM, CRE, CIM);
+            rows_source_loop<ST, SUM, PAIRS, false, MID>(tile_ph, cnt, sm, rt, p0, p2, a0, a1, n0a, U,
+                                                         NP, RE, IM, CRE, CIM);
     }
 
 }
@@ -402,14 +403,14 @@ __device__ __forceinline__ void rows_store(const PackedSource* __restrict__ src,
 }
 
 // One tile of the rows tiling, all n sources, stored.
-template <int ST, int SUM, int PAIRS>
+template <int ST, int SUM, int PAIRS, bool MID = false>
 __device__ __forceinline__ void block_rows(SmemTile& sm, const RowsTable& rt,
                                            const PackedSource* __restrict__ src, int64_t n,
                                            const GridDev& g, int tx_log2, int64_t tiles0,
                                            int64_t tiles1, int64_t tile, int field,
                                            void* __restrict__ out) {
     float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
-    rows_accumulate<ST, SUM, PAIRS>(sm, rt, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE,
+    rows_accumulate<ST, SUM, PAIRS, MID>(sm, rt, src, n, 0, n, g, tx_log2, tiles0, tiles1, tile, RE,
                                     IM, CRE, CIM);
     rows_store<SUM, PAIRS>(src, n, g, tx_log2, tiles0, tiles1, tile, RE, IM, CRE, CIM, field,
                            out);

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         int64_t lo, hi;
         chunk_range(J, w.chunk, lo, hi);
         float2 RE[P], IM[P], CRE[P], CIM[P];
-        rows_accumulate<ST, SUM_PLAIN, P>(sm, rt, J.packed, J.n, lo, hi, J.g, J.tx_log2, J.tiles0,
+        rows_accumulate<ST, SUM_PLAIN, P, true>(sm, rt, J.packed, J.n, lo, hi, J.g, J.tx_log2, J.tiles0,
                                           J.tiles1, w.tile, RE, IM, CRE, CIM);
         if (J.chunks == 1) {
             rows_store<SUM_PLAIN, P>(J.packed, J.n, J.g, J.tx_log2, J.tiles0, J.tiles1, w.tile,
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         chunk_range(J, w.chunk, lo, hi);
         const int64_t first = w.tile * (kThreads * kPPT);
         float2 RE[P], IM[P], CRE[P], CIM[P];
-        block_accumulate<ST, SUM_PLAIN, P>(sm, gt, J.packed, J.n, lo, hi, J.is_grid != 0, J.g,
+        block_accumulate<ST, SUM_PLAIN, P, true>(sm, gt, J.packed, J.n, lo, hi, J.is_grid != 0, J.g,
                                            J.pts, J.m, first, RE, IM, CRE, CIM);
         if (J.chunks == 1) {
             block_store<SUM_PLAIN, P>(RE, IM, CRE, CIM, J.packed, J.n, J.is_grid != 0, J.g, J.pts,
