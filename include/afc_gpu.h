@@ -51,7 +51,17 @@ typedef struct AfcGridDesc {
 int32_t AFC_GridDescFromArea(void *grid_handle, int32_t dimension, AfcGridDesc *out);
 
 /* Bytes of device workspace the field calls need for n sources (16-byte aligned buffer); 0 for
- * n >= 2^40, which the field calls reject with AFC_ERR_TOO_LARGE. */
+ * n >= 2^40, which the field calls reject with AFC_ERR_TOO_LARGE.
+ *
+ * Besides that workspace, a field call on 32,768 points or more whose point tiles would leave
+ * the GPU's last wave short (scatter sets and single-row grids of up to about half a million
+ * points against thousands of sources) may take partial-sum scratch of a few bytes per point:
+ * stream-ordered (cudaMallocFromPoolAsync, cudaFreeAsync on the call's stream) from a pool the
+ * library keeps per device, which holds up to 256 MB between calls.  No scratch is taken while
+ * the stream is being captured into a graph, by the compensated sum (sum_mode 1), by
+ * AFC_FieldGridDeviceNoAlloc, or by the serving engine; those launches, and any call whose
+ * scratch cannot be had, split the sources over thread-block clusters instead.  AFC_Calculate
+ * behaves the same way. */
 size_t AFC_FieldWorkspaceBytes(uint64_t n_sources);
 
 /* Field of n sources on a grid.  d_out receives count[0]*count[1]*count[2] floats (pressure,
