@@ -675,12 +675,24 @@ std::atomic<uint64_t> g_launches{0};
 RowsTiling rows_tiling(const GridDev& g, int64_t m, int pairs) {
     RowsTiling t{false, 5, 0, 0, 0, 0};
     if (g.count[1] <= 1 || m <= 0) return t;
-    // first-axis tile: the smallest power of two >= count[0], between 32 and kThreads
-    while (t.tx_log2 < 8 && (1LL << t.tx_log2) < g.count[0]) ++t.tx_log2;
-    t.rows = (static_cast<int64_t>(kThreads) >> t.tx_log2) * 2 * pairs;
-    t.tiles0 = (g.count[0] + (1LL << t.tx_log2) - 1) >> t.tx_log2;
-    t.tiles1 = (g.count[1] + t.rows - 1) / t.rows;
-    t.blocks = t.tiles0 * t.tiles1 * g.count[2];
+    // first-axis tile: the power of two between 32 and kThreads (at most the smallest one >=
+    // count[0]) whose tiles leave the fewest threads past the grid's edges; on a tie the wider
+    // (a 592 x 592 slice: 19 x 32 = 608 columns of 64-row tiles, where 256 would take 768)
+    int top = 5;
+    while (top < 8 && (1LL << top) < g.count[0]) ++top;
+    for (int k = top; k >= 5; --k) {
+        const int64_t rows = (static_cast<int64_t>(kThreads) >> k) * 2 * pairs;
+        const int64_t tiles0 = (g.count[0] + (1LL << k) - 1) >> k;
+        const int64_t tiles1 = (g.count[1] + rows - 1) / rows;
+        const int64_t blocks = tiles0 * tiles1 * g.count[2];
+        if (k == top || blocks < t.blocks) {
+            t.tx_log2 = k;
+            t.rows = rows;
+            t.tiles0 = tiles0;
+            t.tiles1 = tiles1;
+            t.blocks = blocks;
+        }
+    }
     // the tiles leave the threads past the grid's edges idle: take them only while they keep
     // at least 90 % as many threads busy as the flat numbering does
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * pairs;
