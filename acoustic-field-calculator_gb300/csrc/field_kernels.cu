@@ -175,6 +175,21 @@ struct ChunkSplit {
     }
 };
 
+// The point tile of point q: blocks of tile_points consecutive points (flat numbering), or the
+// rows tiling's tiles (tx_log2 > 0: 1 << tx_log2 first-axis indices by `rows` second-axis
+// indices of one plane, numbered as rows_accumulate numbers them).
+struct TileMap {
+    int tx_log2;
+    int64_t tile_points;
+    int64_t rows, tiles0, tiles1, c0, c1;
+    __device__ __forceinline__ int64_t tile_of(int64_t q) const {
+        if (tx_log2 == 0) return q / tile_points;
+        const int64_t i0 = q % c0, rest = q / c0;
+        const int64_t i1 = rest % c1, i2 = rest / c1;
+        return (i0 >> tx_log2) + tiles0 * (i1 / rows + tiles1 * i2);
+    }
+};
+
 // Persistent chunked launch of the general body for launches whose point tiles alone would
 // leave the last wave short.  A block's items of one tile are consecutive chunks, i.e. one
 // source range: a segment, summed by one block_accumulate pass.  A tile's segments are
@@ -216,17 +231,63 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
+// The same over the rows tiling's tiles (rows_accumulate): a segment writes its sums at its
+// tile's grid points.
+template <int ST, int PAIRS>
+__global__ void __launch_bounds__(kThreads, 2)
+    field_rows_chunk_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                            int tx_log2, int64_t tiles0, int64_t tiles1, int64_t m, ChunkSplit cs,
+                            float2* __restrict__ partial) {
+    constexpr int kPPT = 2 * PAIRS;
+    __shared__ RowsSmem rs;
+    SmemTile& sm = rs.sm;
+    RowsTable& rt = rs.rt;
+    load_theta_table(sm, c_dir_table);
+    load_rows_table(rt);
+    const int tx = threadIdx.x & ((1 << tx_log2) - 1);
+    const int ty = threadIdx.x >> tx_log2;
+    const int64_t c0 = g.count[0], c1 = g.count[1];
+    const int64_t end = cs.start(blockIdx.x + 1);
+    for (int64_t it = cs.start(blockIdx.x); it < end;) {
+        const int64_t tile = it / cs.chunks;
+        const int64_t tile_end = (tile + 1) * cs.chunks;
+        const int64_t seg_end = end < tile_end ? end : tile_end;
+        const int64_t ca = it - tile * cs.chunks, cb = seg_end - tile * cs.chunks;
+        const int64_t lo = ca * cs.chunk < n ? ca * cs.chunk : n;
+        const int64_t hi = cb * cs.chunk < n ? cb * cs.chunk : n;
+        const int64_t k = cs.block_of(it) - cs.block_of(tile * cs.chunks);
+        float2 RE[PAIRS], IM[PAIRS], CRE[PAIRS], CIM[PAIRS];
+        rows_accumulate<ST, SUM_PLAIN, PAIRS>(sm, rt, src, n, lo, hi, g, tx_log2, tiles0, tiles1,
+                                              tile, RE, IM, CRE, CIM);
+        const int64_t t0 = tile % tiles0, rest = tile / tiles0;
+        const int64_t t1 = rest % tiles1, i2 = rest / tiles1;
+        const int64_t i0 = (t0 << tx_log2) + tx;
+        const int64_t i1b = (t1 * (kThreads >> tx_log2) + ty) * kPPT;
+        if (i0 < c0) {
+            float2* part = partial + k * m;
+#pragma unroll
+            for (int j = 0; j < kPPT; ++j) {
+                const int64_t i1 = i1b + j;
+                if (i1 >= c1) break;
+                part[(i2 * c1 + i1) * c0 + i0] =
+                    make_float2(lane_of(RE[j >> 1], j & 1), lane_of(IM[j >> 1], j & 1));
+            }
+        }
+        it = seg_end;
+    }
+}
+
 // The fields of a chunked launch: each point's segment sums added in segment order, the field
 // transform, and the coincident-source fix-up of the single-pass kernels for NaN sums.
 template <bool GRID>
 __global__ void __launch_bounds__(256)
-    field_chunk_combine_kernel(const float2* __restrict__ partial, ChunkSplit cs,
-                               int64_t tile_points, const PackedSource* __restrict__ src,
-                               int64_t n, GridDev g, const float* __restrict__ pts, int64_t m,
-                               int field, void* __restrict__ out) {
+    field_chunk_combine_kernel(const float2* __restrict__ partial, ChunkSplit cs, TileMap tm,
+                               const PackedSource* __restrict__ src, int64_t n, GridDev g,
+                               const float* __restrict__ pts, int64_t m, int field,
+                               void* __restrict__ out) {
     for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < m;
          q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t t0 = (q / tile_points) * cs.chunks;
+        const int64_t t0 = tm.tile_of(q) * cs.chunks;
         const int64_t segs = cs.block_of(t0 + cs.chunks - 1) - cs.block_of(t0) + 1;
         float re = 0.f, im = 0.f;
         for (int64_t k = 0; k < segs; ++k) {
@@ -392,20 +453,19 @@ constexpr int64_t kChunkMaxBytes = 256LL << 20;
 // Its source iterations ran 2.5 % slower than the single-pass kernel's at full waves (4,194,304
 // points: 0.688 against 0.671 us).  A launch of several waves loses less to a short last wave
 // than the wave count says (the blocks of that wave share their SMs with fewer others and run
-// faster), so the chunked launch does not replace one of two or more waves that fills at least
-// 90 % of its slots; it is taken only at 4 point pairs per thread, where it was calibrated.
+// faster: 1,048,576 points in 7 cluster-split waves took 2 % less than modelled), so against a
+// launch of two or more waves the chunked one must model kMultiWaveMargin cheaper.  It is taken
+// only at 4 point pairs per thread, where it was calibrated.
 constexpr double kPassSetup = 11.0;
 constexpr double kChunkFixedUs = 20.0;
 constexpr double kChunkIterationUs = 0.688;
 constexpr double kChunkSlowdown = 1.025;
-constexpr double kChunkBelowFill = 0.9;
+constexpr double kMultiWaveMargin = 0.97;
 
-// whether `blocks` blocks on `slots` resident ones run two or more waves that keep at least
-// kChunkBelowFill of the slots busy
-bool full_waves(int64_t blocks, int64_t slots) {
-    const int64_t waves = (blocks + slots - 1) / slots;
-    return waves >= 2 && static_cast<double>(blocks) >=
-                             kChunkBelowFill * static_cast<double>(waves * slots);
+// the cost the chunked launch must beat: `cost` of a launch of `blocks` blocks on `slots`
+// resident ones, less kMultiWaveMargin when that launch runs two or more waves
+double chunk_bar(double cost, int64_t blocks, int64_t slots) {
+    return (blocks + slots - 1) / slots >= 2 ? kMultiWaveMargin * cost : cost;
 }
 
 // one pass per tile (field_direct_kernel) on `slots` resident blocks
@@ -492,7 +552,8 @@ constexpr int gtab_bytes() {
 // (nothing was launched).
 template <int ST, bool GRID, int PAIRS>
 cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& ps, int field,
-                           void* out, cudaStream_t s, int64_t tiles, int64_t blocks) {
+                           void* out, cudaStream_t s, int64_t tiles, int64_t blocks,
+                           const RowsTiling* rows = nullptr) {
     constexpr int kDyn = gtab_bytes<ST>();
     int64_t slots = 0;
     const ChunkSplit cs = chunk_split(tiles, n, blocks, &slots);
@@ -503,10 +564,20 @@ cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& p
         (void)cudaGetLastError();
         return cudaErrorMemoryAllocation;
     }
-    cudaError_t e = allow_dynamic_smem<field_chunk_kernel<ST, GRID, PAIRS>>(kDyn);
-    if (e == cudaSuccess) {
-        const int64_t items = tiles * cs.chunks;
-        field_chunk_kernel<ST, GRID, PAIRS><<<static_cast<unsigned>(blocks < items ? blocks : items), kThreads, kDyn, s>>>(
+    const int64_t items = tiles * cs.chunks;
+    const unsigned grid_blocks = static_cast<unsigned>(blocks < items ? blocks : items);
+    TileMap tm{0, static_cast<int64_t>(kThreads) * 2 * PAIRS, 0, 0, 0, 0, 0};
+    cudaError_t e = cudaSuccess;
+    if (rows) {
+        tm = TileMap{rows->tx_log2, 0, rows->rows, rows->tiles0, rows->tiles1,
+                     static_cast<int64_t>(ps.grid.count[0]), static_cast<int64_t>(ps.grid.count[1])};
+        field_rows_chunk_kernel<ST, PAIRS><<<grid_blocks, kThreads, 0, s>>>(
+            src, n, ps.grid, rows->tx_log2, rows->tiles0, rows->tiles1, ps.m, cs,
+            static_cast<float2*>(partial));
+        count_launch();
+        e = cudaGetLastError();
+    } else if ((e = allow_dynamic_smem<field_chunk_kernel<ST, GRID, PAIRS>>(kDyn)) == cudaSuccess) {
+        field_chunk_kernel<ST, GRID, PAIRS><<<grid_blocks, kThreads, kDyn, s>>>(
             src, n, ps.grid, ps.pts, ps.m, cs, static_cast<float2*>(partial));
         count_launch();
         e = cudaGetLastError();
@@ -514,8 +585,7 @@ cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& p
     if (e == cudaSuccess) {
         const int64_t want = (ps.m + 255) / 256, cap = 8LL * num_sms();
         field_chunk_combine_kernel<GRID><<<static_cast<unsigned>(want < cap ? want : cap), 256, 0, s>>>(
-            static_cast<const float2*>(partial), cs, static_cast<int64_t>(kThreads) * 2 * PAIRS,
-            src, n, ps.grid, ps.pts, ps.m, field, out);
+            static_cast<const float2*>(partial), cs, tm, src, n, ps.grid, ps.pts, ps.m, field, out);
         count_launch();
         e = cudaGetLastError();
     }
@@ -530,27 +600,26 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
-    if (PAIRS == 4 && !rows.use && SUM == SUM_PLAIN && scratch_ok && n >= 2 * kChunkSources) {
+    if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (!rows.use && scratch_ok && n >= 2 * kChunkSources) {
         // chunked (not while the stream is being captured: the partial sums are allocated on
-        // the stream) when the model puts it below the single pass and the cluster split and
-        // neither runs full waves
+        // the stream) when the model puts it below the single pass and the cluster split
         cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(s, &cst) == cudaSuccess && cst == cudaStreamCaptureStatusNone) {
             const int64_t slots1 = resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn);
             double other = direct_cost(flat_blocks, n, slots1);
-            bool other_full = full_waves(flat_blocks, slots1);
+            double bar = chunk_bar(other, flat_blocks, slots1);
             for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
                 const int64_t slots = resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(S, kDyn);
                 const double c = split_cost(flat_blocks, n, S, slots);
                 if (c < other) {
                     other = c;
-                    other_full = full_waves(flat_blocks * S, slots);
+                    bar = chunk_bar(c, flat_blocks * S, slots);
                 }
             }
             const int64_t blocks =
                 ps.is_grid ? resident_blocks<field_chunk_kernel<ST, true, PAIRS>>(1, kDyn)
                            : resident_blocks<field_chunk_kernel<ST, false, PAIRS>>(1, kDyn);
-            if (!other_full && chunk_cost(flat_blocks, n, blocks) < other) {
+            if (chunk_cost(flat_blocks, n, blocks) < bar) {
                 const cudaError_t e =
                     ps.is_grid ? launch_chunked<ST, true, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks)
                                : launch_chunked<ST, false, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks);
@@ -601,6 +670,32 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         const RowsTiling& t = rows;
         if (t.use) {
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+            if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (scratch_ok && n >= 2 * kChunkSources) {
+                // the chunked launch over the rows tiles, on the same terms as the flat one
+                cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+                if (cudaStreamIsCapturing(s, &cst) == cudaSuccess &&
+                    cst == cudaStreamCaptureStatusNone) {
+                    const int64_t slots1 = resident_blocks<field_rows_kernel<ST, SUM, PAIRS>>(1, 0);
+                    double other = direct_cost(t.blocks, n, slots1);
+                    double bar = chunk_bar(other, t.blocks, slots1);
+                    for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
+                        const int64_t slots = resident_blocks<field_rows_split_kernel<ST, SUM, PAIRS>>(S, 0);
+                        const double c = split_cost(t.blocks, n, S, slots);
+                        if (c < other) {
+                            other = c;
+                            bar = chunk_bar(c, t.blocks * S, slots);
+                        }
+                    }
+                    const int64_t blocks = resident_blocks<field_rows_chunk_kernel<ST, PAIRS>>(1, 0);
+                    if (chunk_cost(t.blocks, n, blocks) < bar) {
+                        const cudaError_t e = launch_chunked<ST, true, PAIRS>(
+                            src, n, ps, field, out, s, t.blocks, blocks, &t);
+                        if (e != cudaErrorMemoryAllocation) return e;
+                    }
+                } else {
+                    (void)cudaGetLastError();
+                }
+            }
             const int64_t S = split_width(t.blocks, n, [](int64_t w) {
                 return w <= 1 ? resident_blocks<field_rows_kernel<ST, SUM, PAIRS>>(1, 0)
                               : resident_blocks<field_rows_split_kernel<ST, SUM, PAIRS>>(w, 0);

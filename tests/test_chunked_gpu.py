@@ -1,4 +1,5 @@
-"""The chunked launch of the general body (field_chunk_kernel + field_chunk_combine_kernel).
+"""The chunked launches (field_chunk_kernel or field_rows_chunk_kernel, then
+field_chunk_combine_kernel).
 
 Scatter sets whose 2,048-point tiles cannot fill the GPU's resident blocks (tens of tiles against
 3,984 sources) are cut into contiguous ranges of (tile, source) work over persistent blocks:
@@ -10,7 +11,9 @@ so the bar is the same 1e-4 of the peak against the f32 oracle.  Checked here:
   * the field against the oracle at sizes with a ragged last tile, in full and (262,144 points)
     on a seeded subsample;
   * the same inputs give the same bits on every call (the split depends on the device only);
-  * a point on a source comes out non-finite like the reference's (the combine's fix-up).
+  * a point on a source comes out non-finite like the reference's (the combine's fix-up);
+  * grids the rows tiling takes (a 64^3 grid; a 600 x 400 slice, ragged along both axes of its
+    32 x 64 tiles) run the same launch over the rows tiles, checked against the oracle.
 """
 import numpy as np
 import pytest
@@ -85,3 +88,32 @@ def test_chunked_point_on_a_source(gpu):
     keep[hit] = False
     assert np.all(np.isfinite(out[keep]))
     assert rel_err(out[keep], ref[keep]) <= TOL
+
+
+@pytest.mark.parametrize("shape", ["cube64", "slice600x400"])
+def test_chunked_rows_grid(gpu, shape):
+    afc = gpu
+    rng, pos, rec, k, a, s = _array_system(afc, 64 if shape == "cube64" else 600)
+    cen = W.array_center(pos)
+    res = 0.5
+    if shape == "cube64":
+        counts = (64, 64, 64)
+        lo = (float(cen[0]) - 16.0, float(cen[1]) - 16.0, 60.0)
+        g = W.GridSpec(3, [(lo[j], lo[j] + (counts[j] - 0.75) * res) for j in range(3)], res,
+                       (1, 2, 3))
+    else:
+        counts = (600, 400, 1)
+        lo = (float(cen[0]) - 150.0, float(cen[1]) - 100.0, 150.0)
+        g = W.GridSpec(2, [(lo[0], lo[0] + 599.25 * res), (lo[1], lo[1] + 399.25 * res),
+                           (lo[2], lo[2])], res, (1, 2, 3))
+    area = afc.grid_from_spec(g)
+    out, launched = _calc(afc, afc.GpuCalculator(), s, area)
+    assert launched == 3, "expected pack + chunked rows field + combine"
+    glo, ghi = g.lo_hi()
+    pts = O.grid_points(g.dim, glo, ghi, res, (1, 2, 3))
+    assert len(pts) == counts[0] * counts[1] * counts[2] == len(out)
+    idx = np.sort(rng.choice(len(pts), 6000, replace=False))
+    idx[0], idx[-1] = 0, len(pts) - 1
+    err = rel_err(out[idx], O.field_f32(1, rec, k, a, pts[idx], O.FIELD_COMPLEX))
+    print(f"chunked rows grid {shape}: {err:.2e}")
+    assert err <= TOL
