@@ -329,3 +329,56 @@ def test_gspat_f32_restatement_tracks_f64():
     p64 = np.abs(O.field_f64(1, s64, w.k, w.atten, foci))
     assert np.max(np.abs(p32 - p64)) <= 1e-4 * np.max(p64)
     np.testing.assert_array_equal(s32[:, [0, 1, 2, 3, 4, 5, 8]], w.sources[:, [0, 1, 2, 3, 4, 5, 8]])
+
+
+def _focus_points(seed, m=400):
+    rng = np.random.default_rng(seed)
+    cen = W.array_center(W.unit_array())
+    pts = np.empty((m, 3), np.float32)
+    pts[:, 0] = rng.uniform(cen[0] - 60, cen[0] + 60, m)
+    pts[:, 1] = rng.uniform(cen[1] - 60, cen[1] + 60, m)
+    pts[:, 2] = rng.uniform(60, 220, m)
+    return pts
+
+
+def test_doubling_every_amplitude_doubles_the_field_exactly():
+    """uniform_medium.rs:111-128 weights each term by its source's amplitude and sums the terms:
+    scaling every amplitude by two scales every f32 product and partial sum by two exactly (no
+    overflow or subnormal here), so the field doubles bit for bit."""
+    w = W.single_focus()
+    pts = _focus_points(3)
+    p1 = O.field_f32(1, w.sources, w.k, w.atten, pts)
+    s2 = w.sources.copy()
+    s2[:, 6] *= 2.0
+    p2 = O.field_f32(1, s2, w.k, w.atten, pts)
+    np.testing.assert_array_equal(p2.view(np.float32), (2 * p1).view(np.float32))
+
+
+def test_field_types_are_the_complex_sum_transformed():
+    """field_buffer/{power,pressure}_field.rs:35-37: the power field is re*re + im*im of the
+    complex sum (f32, each operation rounded), the pressure field its square root, so both follow
+    bit for bit from the complex field."""
+    w = W.single_focus()
+    pts = _focus_points(4)
+    pc = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_COMPLEX)
+    pw = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_POWER)
+    pr = O.field_f32(1, w.sources, w.k, w.atten, pts, O.FIELD_PRESSURE)
+    re = np.ascontiguousarray(pc.real, dtype=np.float32)
+    im = np.ascontiguousarray(pc.imag, dtype=np.float32)
+    ns = (re * re) + (im * im)  # float32 products and sum, each rounded
+    assert ns.dtype == np.float32
+    np.testing.assert_array_equal(pw, ns)
+    np.testing.assert_array_equal(pr, np.sqrt(ns))
+
+
+def test_superposition_of_two_source_sets():
+    """The field is a sum over sources (uniform_medium.rs:122-128): the field of two source sets
+    together equals the sum of their fields, up to the float association of the sum."""
+    w = W.single_focus()
+    pts = _focus_points(5)
+    half = w.n // 2
+    a = O.field_f32(1, w.sources[:half], w.k[:half], w.atten[:half], pts)
+    b = O.field_f32(1, w.sources[half:], w.k[half:], w.atten[half:], pts)
+    ab = O.field_f32(1, w.sources, w.k, w.atten, pts)
+    peak = float(np.max(np.abs(ab)))
+    assert float(np.max(np.abs(ab - (a + b)))) <= 2e-6 * peak
