@@ -108,3 +108,48 @@ def test_batch_sees_source_edits_between_runs(gpu):
         _check(jobs[0], got, _oracle(jobs[0], _points(jobs[0], pts[0])))
     finally:
         afc.DLL.AFC_BatchFree(plan)
+
+
+def test_batch_far_jobs_take_the_mid_tier(gpu):
+    """Jobs 0.9 m above the 2,490-source array (5 x 2 tiling, 904 mm wide): every tile's phase
+    bound lies between the unreduced path's 640 rad and 1,024 rad, so the batch kernels take
+    their mid phase tier (r refined by a Newton step, the phase fused into one rounding, a
+    packed 2 pi reduction).  Random phases and no attenuation make the sum incoherent, so the
+    field's error is about the per-pair phase error.  A 128 x 128 slice (rows body) and a
+    scatter set (general body) against the oracle at the 1e-4 bar."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    rng = np.random.default_rng(900)
+    pos = W.tiled_array(5, 2)
+    n = len(pos)
+    src = W.t4010a1_records(pos, rng.uniform(0.5, 1.0, n).astype(np.float32),
+                            rng.uniform(0, 2 * np.pi, n).astype(np.float32))
+    k = np.full(n, W.wavenumber(), np.float32)
+    a = np.zeros(n, np.float32)
+    cen = W.array_center(pos)
+    res = 0.5
+    x0, y0 = float(cen[0]) - 32.0, float(cen[1]) - 32.0
+    grid = W.GridSpec(2, [(x0, x0 + 127.25 * res), (y0, y0 + 127.25 * res), (900.0, 900.0)], res,
+                      (1, 2, 3))
+    jobs = [W.BatchJob(src, k, a, 2, grid, 128 * 128, 0, (), ()),
+            W.BatchJob(src, k, a, 2, None, 30000, 901,
+                       (float(cen[0]) - 50.0, float(cen[1]) - 50.0, 880.0),
+                       (float(cen[0]) + 50.0, float(cen[1]) + 50.0, 960.0))]
+    arr, outs, pts, keep = BD.materialize(afc, torch, jobs)
+    st = torch.cuda.current_stream().cuda_stream
+    plan = BD.create_plan(afc, arr, False, st)
+    try:
+        assert afc.DLL.AFC_BatchRun(plan, st) == 0, afc.last_error()
+        torch.cuda.synchronize()
+        for jb, o, p in zip(jobs, outs, pts):
+            pp = _points(jb, p)
+            # the largest source-to-corner distance of the job's points: every tile's bound is
+            # at most this, and the nearest sources are 0.9 m away (k r about 665 rad)
+            lo, hi = pp.min(0).astype(np.float64), pp.max(0).astype(np.float64)
+            corners = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1])
+                                for z in (lo[2], hi[2])])
+            rmax = np.sqrt(((corners[:, None, :] - pos[None, :, :]) ** 2).sum(-1)).max()
+            assert 640.0 < float(k[0]) * rmax + np.pi < 1024.0
+            _check(jb, _as_field(o, 2), _oracle(jb, pp))
+    finally:
+        afc.DLL.AFC_BatchFree(plan)

@@ -13,7 +13,9 @@ so the bar is the same 1e-4 of the peak against the f32 oracle.  Checked here:
   * the same inputs give the same bits on every call (the split depends on the device only);
   * a point on a source comes out non-finite like the reference's (the combine's fix-up);
   * grids the rows tiling takes (a 64^3 grid; a 600 x 400 slice, ragged along both axes of its
-    32 x 64 tiles) run the same launch over the rows tiles, checked against the oracle.
+    32 x 64 tiles) run the same launch over the rows tiles, and a 450 x 300 slice, which the
+    rows tiles would leave 12 % idle, over the flat numbering's tiles; checked against the
+    oracle.
 """
 import numpy as np
 import pytest
@@ -90,10 +92,10 @@ def test_chunked_point_on_a_source(gpu):
     assert rel_err(out[keep], ref[keep]) <= TOL
 
 
-@pytest.mark.parametrize("shape", ["cube64", "slice600x400"])
-def test_chunked_rows_grid(gpu, shape):
+@pytest.mark.parametrize("shape", ["cube64", "slice600x400", "slice450x300"])
+def test_chunked_grid(gpu, shape):
     afc = gpu
-    rng, pos, rec, k, a, s = _array_system(afc, 64 if shape == "cube64" else 600)
+    rng, pos, rec, k, a, s = _array_system(afc, {"cube64": 64, "slice600x400": 600}.get(shape, 450))
     cen = W.array_center(pos)
     res = 0.5
     if shape == "cube64":
@@ -102,18 +104,19 @@ def test_chunked_rows_grid(gpu, shape):
         g = W.GridSpec(3, [(lo[j], lo[j] + (counts[j] - 0.75) * res) for j in range(3)], res,
                        (1, 2, 3))
     else:
-        counts = (600, 400, 1)
+        c0, c1 = (600, 400) if shape == "slice600x400" else (450, 300)
+        counts = (c0, c1, 1)
         lo = (float(cen[0]) - 150.0, float(cen[1]) - 100.0, 150.0)
-        g = W.GridSpec(2, [(lo[0], lo[0] + 599.25 * res), (lo[1], lo[1] + 399.25 * res),
+        g = W.GridSpec(2, [(lo[0], lo[0] + (c0 - 0.75) * res), (lo[1], lo[1] + (c1 - 0.75) * res),
                            (lo[2], lo[2])], res, (1, 2, 3))
     area = afc.grid_from_spec(g)
     out, launched = _calc(afc, afc.GpuCalculator(), s, area)
-    assert launched == 3, "expected pack + chunked rows field + combine"
+    assert launched == 3, "expected pack + chunked field + combine"
     glo, ghi = g.lo_hi()
     pts = O.grid_points(g.dim, glo, ghi, res, (1, 2, 3))
     assert len(pts) == counts[0] * counts[1] * counts[2] == len(out)
     idx = np.sort(rng.choice(len(pts), 6000, replace=False))
     idx[0], idx[-1] = 0, len(pts) - 1
     err = rel_err(out[idx], O.field_f32(1, rec, k, a, pts[idx], O.FIELD_COMPLEX))
-    print(f"chunked rows grid {shape}: {err:.2e}")
+    print(f"chunked grid {shape}: {err:.2e}")
     assert err <= TOL

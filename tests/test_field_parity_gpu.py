@@ -457,10 +457,11 @@ def test_rows_split_mid_size(gpu, calc, tilted):
 def test_far_field_with_random_phases(gpu, dist):
     """Every point 1, 1.5 or 3 m from a 4 x 4 tiling (3,984 sources) driven with random phases,
     no attenuation: the sum is incoherent, so the field's relative error is about the per-pair
-    phase error, which grows with k r.  The far tiles take r through a Newton step and a
-    two-constant 2 pi reduction: at 1 m (phase bounds about 830-900 rad) with the phase fused
-    (the kernels' mid tier, below 1,024 rad), at 1.5 and 3 m rounded as the reference rounds it.
-    Checked against the f32 oracle on a grid and scatter points."""
+    phase error, which grows with k r.  The far tiles take r through a Newton step, the phase
+    rounded as the reference rounds it and a two-constant 2 pi reduction (the single-job
+    kernels' careful tier; the mid tier of the batch and serving kernels, below 1,024 rad, is
+    checked in test_batch_gpu.py).  Checked against the f32 oracle on a grid and scatter
+    points."""
     afc = gpu
     rng = np.random.default_rng(int(dist))
     pos = W.tiled_array(4, 4)
