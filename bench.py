@@ -90,6 +90,9 @@ def parse():
     ap.add_argument("--mp-points", type=int, default=262144, help="multipattern: points")
     ap.add_argument("--mp-patterns", type=int, default=1024, help="multipattern: patterns")
     ap.add_argument("--batch-jobs", type=int, default=2048, help="batch: job count")
+    ap.add_argument("--batch-fixed-plan", action="store_true",
+                    help="batch: the fixed plan (4 point pairs, occupancy blocks per SM) instead of "
+                         "the autotuned one, so that a profiler sees no tuning launches")
     ap.add_argument("--scatter-points", type=int, default=262144,
                     help="scatter: points, drawn uniformly in the multi-pattern box")
     ap.add_argument("--serve-slots", type=int, default=32,
@@ -668,7 +671,7 @@ def run_multipattern(args):
 
 # ------------------------------------------------------------------ batched uneven jobs
 
-def batch_measure(afc, torch, n_jobs, steps, warmup, one_by_one_steps=3):
+def batch_measure(afc, torch, n_jobs, steps, warmup, one_by_one_steps=3, tune=True):
     """n_jobs independent field jobs (249/498/996/2,490 transducers, 1e3-1e6 points, half grid
     slices, half scatter sets) as one persistent launch replayed from a CUDA graph (autotuned
     plan), against the same jobs launched one by one."""
@@ -680,7 +683,7 @@ def batch_measure(afc, torch, n_jobs, steps, warmup, one_by_one_steps=3):
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     t0 = time.perf_counter()
-    plan = BD.create_plan(afc, arr, True, sh)
+    plan = BD.create_plan(afc, arr, tune, sh)
     create_s = time.perf_counter() - t0
     info = BD.describe(afc, plan)
 
@@ -701,7 +704,7 @@ def batch_measure(afc, torch, n_jobs, steps, warmup, one_by_one_steps=3):
     tbm, tem = statistics.median(tb), statistics.median(te)
     return {"workload": f"batch_{len(jobs)}_uneven_jobs", "jobs": len(jobs),
             "evals_per_step": evals, "points_per_step": int(sum(j.n_points for j in jobs)),
-            "autotuned": info, "plan_create_s": create_s,
+            "autotuned": info, "tuned": tune, "plan_create_s": create_s,
             "replay_ms": tbm * 1e3, "evals_per_s": evals / tbm,
             "one_by_one_ms": tem * 1e3, "one_by_one_evals_per_s": evals / tem,
             "one_by_one_launches_per_step": 2 * len(jobs),
@@ -716,7 +719,8 @@ def run_batch(args):
     import afc
 
     afc.DLL.AFC_SetDevice(local)
-    r = batch_measure(afc, torch, args.batch_jobs, args.steps, args.warmup)
+    r = batch_measure(afc, torch, args.batch_jobs, args.steps, args.warmup,
+                      tune=not args.batch_fixed_plan)
     line = {"metric": "source-point evaluations/s (2,048 uneven jobs, one persistent launch)",
             "value": r["evals_per_s"], "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["replay_ms"], "higher_is_better": True,
