@@ -433,12 +433,22 @@ int32_t gpu_calculate(Calculator* calc, System* sys, void* area, int area_type, 
             cudaSuccess)
             return cuda_fail(e, "pack_sources");
     }
-    if ((e = g.out.ensure(out_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(field)");
+    // The kernels write the field straight into the pinned host buffer when the device can
+    // address it (under unified addressing every cudaHostAlloc buffer is, at its host address):
+    // no device-to-host copy after the launch.  Otherwise into device memory, then copied.
+    void* dst = nullptr;
+    const bool to_host = cudaHostGetDevicePointer(&dst, field->host, 0) == cudaSuccess && dst;
+    if (!to_host) {
+        (void)cudaGetLastError();
+        if ((e = g.out.ensure(out_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(field)");
+        dst = g.out.p;
+    }
     if ((e = launch_field(sys->st, ft, sum_mode, static_cast<const PackedSource*>(g.packed.p), n,
-                          ps, g.out.p, g.stream)) != cudaSuccess)
+                          ps, dst, g.stream)) != cudaSuccess)
         return cuda_fail(e, "field kernel launch");
-    if ((e = cudaMemcpyAsync(field->host, g.out.p, out_bytes, cudaMemcpyDeviceToHost, g.stream)) !=
-        cudaSuccess)
+    if (!to_host &&
+        (e = cudaMemcpyAsync(field->host, g.out.p, out_bytes, cudaMemcpyDeviceToHost, g.stream)) !=
+            cudaSuccess)
         return cuda_fail(e, "cudaMemcpyAsync(field)");
     if ((e = cudaStreamSynchronize(g.stream)) != cudaSuccess)
         return cuda_fail(e, "field calculation");
