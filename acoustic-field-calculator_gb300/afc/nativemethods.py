@@ -135,7 +135,8 @@ NEW_EXPORTS = [
     "AFC_FieldScatterDevice", "AFC_KernelLaunchCount", "AFC_CudaDeviceCount",
     "AFC_MeasurePipeRates", "AFC_SetDevice", "AFC_FieldGridDeviceNoAlloc",
     "AFC_MultiPatternWorkspaceBytes", "AFC_MultiPatternBuildG", "AFC_MultiPatternApply",
-    "AFC_MultiPatternStatus", "AFC_MultiPatternDirect", "AFC_BatchCreate", "AFC_BatchRun",
+    "AFC_MultiPatternStatus", "AFC_MultiPatternApplyWaitTest", "AFC_MultiPatternDirect",
+    "AFC_BatchCreate", "AFC_BatchRun",
     "AFC_BatchRunOneByOne", "AFC_BatchDescribe", "AFC_BatchDescribeKernels", "AFC_BatchFree",
     "AFC_ServeCreate",
     "AFC_ServeAddGeometry", "AFC_ServeSubmitField", "AFC_ServeSubmitGspat", "AFC_ServeWait",
@@ -288,6 +289,8 @@ def __init_new():
     AFC_DLL.AFC_MultiPatternStatus.argtypes = [c_int32, c_uint64, c_uint64, c_uint64, c_void_p,
                                                c_void_p]
     AFC_DLL.AFC_MultiPatternStatus.restype = c_int32
+    AFC_DLL.AFC_MultiPatternApplyWaitTest.argtypes = AFC_DLL.AFC_MultiPatternApply.argtypes
+    AFC_DLL.AFC_MultiPatternApplyWaitTest.restype = c_int32
     AFC_DLL.AFC_MultiPatternDirect.argtypes = [c_int32, c_void_p, c_void_p, c_void_p, c_uint64,
                                                c_void_p, c_uint64, c_void_p, c_void_p, c_uint64,
                                                c_void_p, c_void_p, c_size_t, c_void_p]

@@ -77,7 +77,11 @@ struct GemmCfg {
 static_assert(GemmCfg<true>::kSmemBytes <= 227 * 1024 && GemmCfg<false>::kSmemBytes <= 227 * 1024,
               "GEMM ring exceeds the shared memory of a CTA");
 static_assert((2 * GemmCfg<false>::kStages + 5) * 8 + 8 <= 256, "GEMM barriers exceed their area");
-constexpr uint32_t kWaitLimit = 1u << 24;
+// Every mbarrier wait gives up after kWaitNs of the global timer (a second: far beyond any stage's
+// or tile's wait in a run that works; a tile's MMAs take about 0.1 ms), so that a kernel whose
+// pipeline stalled returns an error code instead of hanging.  kWaitPolls backs the timer up.
+constexpr uint64_t kWaitNs = 1000000000ull;
+constexpr uint32_t kWaitPolls = 1u << 30;
 
 enum : unsigned { ERR_NONE = 0, ERR_TIMEOUT_PRODUCER = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_EPILOGUE = 3 };
 
@@ -99,19 +103,32 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
-// Wait until the phase with the given parity has completed; false after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait until the phase with the given parity has completed; false once kWaitNs have passed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t addr = smem_u32(bar);
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
-        uint32_t ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (ok) return true;
+    if (mbar_try(addr, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 0; i < kWaitPolls; ++i) {
+        if (mbar_try(addr, parity)) return true;
+        if (global_ns() - t0 > kWaitNs) return false;
     }
     return false;
 }
@@ -230,6 +247,7 @@ struct GemmArgs {
     int64_t tiles;       // output tiles in all (BM-row tiles x n_tiles)
     const float* row_scale;  // nullable: C row i multiplied by row_scale[i]
     unsigned* err;       // error code (first writer wins)
+    int stall;           // testing: the producer arms no stage, so that every wait runs out
 };
 
 // Persistent: CTA pair p computes output tiles p, p + pairs, ... (tile t = row tile t / n_tiles,
@@ -289,7 +307,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            int it = 0;  // K blocks issued over all of this CTA's tiles
+            int it = 0;     // K blocks over all of this CTA's tiles
+            int armed = 0;  // of those, the ones whose copies were issued
             bool ok = true;
             for (int64_t t = first; ok && t < args.tiles; t += stride) {
                 const int a_row = static_cast<int>(t / args.n_tiles) * BM + static_cast<int>(rank) * HALF;
@@ -302,6 +321,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                         ok = false;
                         break;
                     }
+                    if (args.stall) continue;
                     uint8_t* st = smem + s * Cfg::kStageBytes;
                     const uint32_t bar = cluster_addr(&full[s], 0);
                     // rank 0 arms its barrier with the bytes of both CTAs' copies
@@ -311,9 +331,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     if (BF16) tma_load_2d_pair(st + OP_TILE, &map_a1, bar, k, a_row);
                     tma_load_2d_pair(st + Cfg::kPlanes * OP_TILE, &map_b0, bar, k, b_row);
                     if (BF16) tma_load_2d_pair(st + 3 * OP_TILE, &map_b1, bar, k, b_row);
+                    armed = it + 1;
                 }
             }
-            *issued_slot = it;
+            *issued_slot = armed;
         }
     } else if (warp == 1) {
         if (rank == 0 && lane == 0) {
@@ -770,10 +791,11 @@ extern "C" int32_t AFC_MultiPatternBuildG(int32_t source_type, int32_t precision
     return AFC_OK;
 }
 
-extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
-                                         const float* d_phases, uint64_t n, uint64_t m,
-                                         uint64_t patterns, float* d_out, void* d_ws,
-                                         size_t ws_bytes, void* stream) {
+namespace {
+
+int32_t multipattern_apply(int32_t precision, const float* d_amps, const float* d_phases,
+                           uint64_t n, uint64_t m, uint64_t patterns, float* d_out, void* d_ws,
+                           size_t ws_bytes, void* stream, int stall) {
     if (precision != AFC_PRECISION_BF16X3 && precision != AFC_PRECISION_FP16) {
         set_error_message("AFC_MultiPatternApply: invalid precision");
         return AFC_ERR_INVALID;
@@ -855,6 +877,7 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
     a.err = err;
     a.n_tiles = static_cast<int>(L.npad / BN);
     a.tiles = static_cast<int64_t>(a.n_tiles) * ((mm + BM - 1) / BM);
+    a.stall = stall;
     e = split ? launch_gemm<true>(ma0, ma1, mb0, mb1, a, dev, s)
               : launch_gemm<false>(ma0, ma1, mb0, mb1, a, dev, s);
     if (e != cudaSuccess) {
@@ -874,6 +897,27 @@ extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
         return AFC_ERR_CUDA;
     }
     return AFC_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t AFC_MultiPatternApply(int32_t precision, const float* d_amps,
+                                         const float* d_phases, uint64_t n, uint64_t m,
+                                         uint64_t patterns, float* d_out, void* d_ws,
+                                         size_t ws_bytes, void* stream) {
+    return multipattern_apply(precision, d_amps, d_phases, n, m, patterns, d_out, d_ws, ws_bytes,
+                              stream, 0);
+}
+
+// Testing: AFC_MultiPatternApply with the GEMM's producer arming no pipeline stage, so that every
+// mbarrier wait of the kernel runs out (about a second) and the kernel returns through its error
+// path.  The output is not computed.
+extern "C" int32_t AFC_MultiPatternApplyWaitTest(int32_t precision, const float* d_amps,
+                                                 const float* d_phases, uint64_t n, uint64_t m,
+                                                 uint64_t patterns, float* d_out, void* d_ws,
+                                                 size_t ws_bytes, void* stream) {
+    return multipattern_apply(precision, d_amps, d_phases, n, m, patterns, d_out, d_ws, ws_bytes,
+                              stream, 1);
 }
 
 // Error code left by the last AFC_MultiPatternApply in this workspace (0: none, 1-3: an

@@ -103,10 +103,18 @@ int32_t AFC_MultiPatternApply(int32_t precision, const float *d_amps, const floa
                               uint64_t n, uint64_t m, uint64_t patterns, float *d_out,
                               void *d_workspace, size_t workspace_bytes, void *stream);
 /* 0 if the last AFC_MultiPatternApply in this workspace completed, else the code of the
- * tensor-core pipeline stage whose bounded wait expired (1 loader, 2 MMA, 3 epilogue).
- * Synchronises the stream. */
+ * tensor-core pipeline stage whose bounded wait (a second of the GPU's global timer) expired
+ * first (1 loader, 2 MMA, 3 epilogue).  Synchronises the stream. */
 int32_t AFC_MultiPatternStatus(int32_t precision, uint64_t n, uint64_t m, uint64_t patterns,
                                void *d_workspace, void *stream);
+/* Testing the bounded waits: AFC_MultiPatternApply with the GEMM's loader arming no pipeline
+ * stage, so that every wait of the kernel runs out and it returns through its error path (about
+ * a second; the output is not computed).  AFC_MultiPatternStatus then reports a nonzero code,
+ * and the workspace and context stay usable. */
+int32_t AFC_MultiPatternApplyWaitTest(int32_t precision, const float *d_amps,
+                                      const float *d_phases, uint64_t n, uint64_t m,
+                                      uint64_t patterns, float *d_out, void *d_workspace,
+                                      size_t workspace_bytes, void *stream);
 /* The same P by FP32 direct summation, one field evaluation per pattern, written pattern-major
  * (P[i][k] at d_out[2 (k m + i)]); workspace of 2 * AFC_FieldWorkspaceBytes(n) bytes. */
 int32_t AFC_MultiPatternDirect(int32_t source_type, const float *d_sources,

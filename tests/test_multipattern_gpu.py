@@ -151,3 +151,42 @@ def test_multipattern_full_size_sampled_rows_vs_f64(gpu):
         print(f"full size precision {prec}: max {e[0]:.2e} rel-L2 {e[1]:.2e}")
         assert e[0] <= bar
         del ws, out
+
+
+def test_gemm_waits_run_out_and_report(gpu):
+    """The tensor-core GEMM's mbarrier waits are bounded (a second of the global timer).  Run with
+    its loader arming no pipeline stage (AFC_MultiPatternApplyWaitTest: a barrier nothing
+    completes), every wait runs out, the kernel records which role gave up first, frees its
+    tensor memory and returns; the next apply in the same workspace and context is correct."""
+    torch = pytest.importorskip("torch")
+    import time
+
+    afc = gpu
+    src, k, a, pts, amps, phases = _problem(9, (1, 1), 700, 40)
+    n, m, K = len(k), len(pts), len(amps)
+    dev = "cuda"
+    d = [torch.from_numpy(x.reshape(-1)).to(dev) for x in (src, k, a, pts, amps, phases)]
+    wsb = afc.DLL.AFC_MultiPatternWorkspaceBytes(n, m, K, BF16X3)
+    ws = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
+    base = (ws.data_ptr() + 255) // 256 * 256
+    out = torch.zeros(2 * m * K, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    assert afc.DLL.AFC_MultiPatternBuildG(1, BF16X3, d[0].data_ptr(), d[1].data_ptr(),
+                                          d[2].data_ptr(), n, d[3].data_ptr(), m, K, base, wsb,
+                                          st) == 0, afc.last_error()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    assert afc.DLL.AFC_MultiPatternApplyWaitTest(BF16X3, d[4].data_ptr(), d[5].data_ptr(), n, m,
+                                                 K, out.data_ptr(), base, wsb, st) == 0
+    code = afc.DLL.AFC_MultiPatternStatus(BF16X3, n, m, K, base, st)
+    stalled_s = time.perf_counter() - t0
+    assert code in (1, 2, 3), code
+    assert stalled_s < 30.0
+    # the same workspace and context afterwards
+    assert afc.DLL.AFC_MultiPatternApply(BF16X3, d[4].data_ptr(), d[5].data_ptr(), n, m, K,
+                                         out.data_ptr(), base, wsb, st) == 0, afc.last_error()
+    assert afc.DLL.AFC_MultiPatternStatus(BF16X3, n, m, K, base, st) == 0
+    got = out.cpu().numpy().view(np.complex64).reshape(m, K)
+    e, _ = _errs(got, _p64(src, k, a, pts, amps, phases))
+    print(f"stalled apply: code {code} after {stalled_s:.2f} s; next apply {e:.2e}")
+    assert e <= 1e-4
