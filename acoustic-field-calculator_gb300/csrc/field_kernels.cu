@@ -29,10 +29,15 @@
 //     operations per pair instead of four.  Each block decides this per tile.
 //   * Each of the 2*PAIRS stores is one contiguous, coalesced warp store (4 B or 8 B a point).
 //   * Grid points are generated from the grid description, never read from memory.
-//   * Launches too small to give every SM two blocks split each point tile's sources over the
-//     blocks of a thread-block cluster (field_split_kernel): rank r sums its share of the
-//     sources, and rank 0 adds the others' partial sums, read from their shared memory, in
-//     rank order -- deterministic, no workspace.
+//   * Launches whose tiles would leave the last wave short either split each point tile's
+//     sources over the blocks of a thread-block cluster (field_split_kernel,
+//     field_rows_split_kernel): rank r sums its share of the sources, and rank 0 adds the
+//     others' partial sums, read from their shared memory, in rank order -- deterministic, no
+//     workspace; or, with scratch for partial sums, run the chunked launch (field_chunk_kernel,
+//     field_rows_chunk_kernel): persistent blocks over contiguous ranges of the (tile, source)
+//     pairs, whose partial sums a second launch adds in source order.  A cost model
+//     (direct_cost, split_cost, chunk_cost) picks among the single pass, the split and the
+//     chunked launch.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
