@@ -106,9 +106,16 @@ class DeviceGuard {
     bool switched_ = false;
 };
 
-// The device whose work `s` orders (the current device for the default stream, NULL).
+// The device whose work `s` orders (the current device for the default stream, NULL).  While
+// `s` is being captured into a graph cudaStreamGetDevice is refused (in the global and thread-
+// local capture modes), so the current device is taken: a capture records work of the current
+// device's context.
 inline cudaError_t stream_device(cudaStream_t s, int* dev) {
-    return s ? cudaStreamGetDevice(s, dev) : cudaGetDevice(dev);
+    if (!s) return cudaGetDevice(dev);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+        return cudaGetDevice(dev);
+    return cudaStreamGetDevice(s, dev);
 }
 
 // Record `msg` as this thread's last error (read back by AFC_GetLastError).

@@ -120,3 +120,43 @@ def test_chunked_grid(gpu, shape):
     err = rel_err(out[idx], O.field_f32(1, rec, k, a, pts[idx], O.FIELD_COMPLEX))
     print(f"chunked grid {shape}: {err:.2e}")
     assert err <= TOL
+
+
+def test_stream_capture_falls_back_to_the_cluster_split(gpu):
+    """Under stream capture the chunked launch cannot take its partial sums from the stream, so a
+    launch it would take runs as the cluster split inside the graph: the replayed graph's field
+    matches the oracle and the eager (chunked) launch's to the parity bar."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    rng, pos, rec, k, a, s = _array_system(afc, 77)
+    m = 65_536
+    pts = W.scatter_box(77, m, W.array_center(pos)[:2])
+    d_src, d_k, d_a, d_pts = (torch.from_numpy(x.reshape(-1)).cuda() for x in (rec, k, a, pts))
+    n = len(k)
+    wsb = afc.DLL.AFC_FieldWorkspaceBytes(n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    eager = torch.empty(2 * m, dtype=torch.float32, device="cuda")
+    captured = torch.full((2 * m,), float("nan"), dtype=torch.float32, device="cuda")
+
+    def field(out, stream):
+        return afc.DLL.AFC_FieldScatterDevice(1, 2, 0, d_src.data_ptr(), d_k.data_ptr(),
+                                              d_a.data_ptr(), n, d_pts.data_ptr(), m,
+                                              out.data_ptr(), ws.data_ptr(), wsb, stream)
+
+    n0 = afc.DLL.AFC_KernelLaunchCount()
+    assert field(eager, torch.cuda.current_stream().cuda_stream) == 0, afc.last_error()
+    assert afc.DLL.AFC_KernelLaunchCount() - n0 == 3  # pack + chunked field + combine
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        n0 = afc.DLL.AFC_KernelLaunchCount()
+        assert field(captured, torch.cuda.current_stream().cuda_stream) == 0, afc.last_error()
+        assert afc.DLL.AFC_KernelLaunchCount() - n0 == 2  # pack + cluster split
+    graph.replay()
+    torch.cuda.synchronize()
+    got_c = captured.cpu().numpy().view(np.complex64)
+    got_e = eager.cpu().numpy().view(np.complex64)
+    idx = np.sort(rng.choice(m, 4000, replace=False))
+    ref = O.field_f32(1, rec, k, a, pts[idx], O.FIELD_COMPLEX)
+    assert rel_err(got_c[idx], ref) <= TOL
+    assert rel_err(got_c, got_e) <= TOL
