@@ -676,9 +676,7 @@ cudaError_t launch_gemm(const CUtensorMap& ma0, const CUtensorMap& ma1, const CU
                         const CUtensorMap& mb1, const GemmArgs& a, int dev, cudaStream_t s) {
     using Cfg = GemmCfg<BF16>;
     auto* kern = cgemm_tcgen05_kernel<BF16>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         Cfg::kSmemBytes);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 2;
@@ -694,6 +692,11 @@ cudaError_t launch_gemm(const CUtensorMap& ma0, const CUtensorMap& ma1, const CU
                     ? g_gemm_pairs[dev][BF16 ? 1 : 0].load(std::memory_order_relaxed)
                     : 0;
     if (pairs <= 0) {
+        // first call on this device: the shared-memory opt-in and the co-resident pairs (both
+        // kept, so that later calls, also under stream capture, make neither query)
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Cfg::kSmemBytes)) != cudaSuccess)
+            return e;
         cfg.gridDim = dim3(2 * static_cast<unsigned>(num_sms() / 2));
         if ((e = cudaOccupancyMaxActiveClusters(&pairs, kern, &cfg)) != cudaSuccess) return e;
         if (pairs < 1) return cudaErrorInvalidConfiguration;

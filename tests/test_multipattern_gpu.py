@@ -190,3 +190,37 @@ def test_gemm_waits_run_out_and_report(gpu):
     e, _ = _errs(got, _p64(src, k, a, pts, amps, phases))
     print(f"stalled apply: code {code} after {stalled_s:.2f} s; next apply {e:.2e}")
     assert e <= 1e-4
+
+
+def test_apply_captured_in_a_graph_matches_eager(gpu):
+    """AFC_MultiPatternApply recorded into a CUDA graph (torch.cuda.graph, global capture mode)
+    and replayed gives the eager apply's bits: the CTA-pair GEMM's cluster launch, its
+    operand builds and its shared-memory opt-in are all capture-safe after the first call."""
+    torch = pytest.importorskip("torch")
+    afc = gpu
+    src, k, a, pts, amps, phases = _problem(12, (1, 1), 900, 48)
+    n, m, K = len(k), len(pts), len(amps)
+    d = [torch.from_numpy(x.reshape(-1)).cuda() for x in (src, k, a, pts, amps, phases)]
+    for prec in (BF16X3, FP16):
+        wsb = afc.DLL.AFC_MultiPatternWorkspaceBytes(n, m, K, prec)
+        ws = torch.empty(wsb + 256, dtype=torch.uint8, device="cuda")
+        base = (ws.data_ptr() + 255) // 256 * 256
+        eager = torch.zeros(2 * m * K, dtype=torch.float32, device="cuda")
+        replayed = torch.full((2 * m * K,), float("nan"), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        assert afc.DLL.AFC_MultiPatternBuildG(1, prec, d[0].data_ptr(), d[1].data_ptr(),
+                                              d[2].data_ptr(), n, d[3].data_ptr(), m, K, base,
+                                              wsb, st) == 0, afc.last_error()
+        assert afc.DLL.AFC_MultiPatternApply(prec, d[4].data_ptr(), d[5].data_ptr(), n, m, K,
+                                             eager.data_ptr(), base, wsb, st) == 0
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            rc = afc.DLL.AFC_MultiPatternApply(prec, d[4].data_ptr(), d[5].data_ptr(), n, m, K,
+                                               replayed.data_ptr(), base, wsb,
+                                               torch.cuda.current_stream().cuda_stream)
+            assert rc == 0, afc.last_error()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert afc.DLL.AFC_MultiPatternStatus(prec, n, m, K, base, st) == 0
+        np.testing.assert_array_equal(replayed.cpu().numpy(), eager.cpu().numpy())
