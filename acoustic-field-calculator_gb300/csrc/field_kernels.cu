@@ -749,20 +749,30 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     return cudaGetLastError();
 }
 
-// Points per thread, the cluster split refilling the waves.  Grids with more than one point
-// along their second axis, whose rows body shares two coordinates per thread: 4 point pairs
-// from 131,072 points and 2 from 32,768 (40^3, 64^3 and 80^3 grids ran 4-9 % faster than with
-// fewer pairs).  Scatter points and single-row grids: 4 point pairs from 32,768 points, one
-// below (3,984 sources: 65,536 points ran 24 % and 262,144 points 2 % faster with 4 pairs
-// than with one; 16,384 points ran 40 % slower with 2 pairs than with one, its 16 tiles too
-// few even split 8 ways).
+// Points per thread, the cluster split or the chunked launch refilling the waves.  Scatter
+// points and single-row grids: 4 point pairs from 32,768 points, one below (3,984 sources:
+// 65,536 points ran 24 % and 262,144 points 2 % faster with 4 pairs than with one; 16,384
+// points ran 40 % slower with 2 pairs than with one, its 16 tiles too few even split 8 ways).
+// Grids with more than one point along their second axis, whose rows body shares two
+// coordinates per thread: 4 point pairs from 32,768 points where the chunked launch is open
+// (scratch allowed, no stream capture; 3,984 sources: 40^3 and 48^3 grids ran 12 % and 6 %
+// faster, 200^2, 256^2 and 360^2 slices 19-25 %), else from 131,072 points and 2 from 32,768
+// (40^3, 64^3 and 80^3 grids ran 4-9 % faster than with fewer pairs under the cluster split).
 template <int ST>
 cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
                       int field, void* out, cudaStream_t s, bool scratch_ok) {
     if (sum_mode == SUM_COMPENSATED)
         return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s, false);
+    bool chunk_open = scratch_ok;
+    if (chunk_open) {
+        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cst) != cudaSuccess || cst != cudaStreamCaptureStatusNone) {
+            (void)cudaGetLastError();
+            chunk_open = false;
+        }
+    }
     const bool rows_grid = ps.is_grid && ps.grid.count[1] > 1;  // the rows body can take it
-    const int64_t four_from = rows_grid ? 131072 : 32768;
+    const int64_t four_from = (rows_grid && !chunk_open) ? 131072 : 32768;
     const int64_t two_from = rows_grid ? 32768 : INT64_MAX;
     if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s, scratch_ok);
     if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s, scratch_ok);
