@@ -753,6 +753,8 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
 // points and single-row grids: 4 point pairs from 32,768 points, one below (3,984 sources:
 // 65,536 points ran 24 % and 262,144 points 2 % faster with 4 pairs than with one; 16,384
 // points ran 40 % slower with 2 pairs than with one, its 16 tiles too few even split 8 ways).
+// Where the chunked launch is open, point sets from 2,048 points against at least 1,024
+// sources (and 5e6 evaluations) take 4 point pairs too (below).
 // Grids with more than one point along their second axis, whose rows body shares two
 // coordinates per thread: 4 point pairs from 32,768 points where the chunked launch is open
 // (scratch allowed, no stream capture; 3,984 sources: 40^3 and 48^3 grids ran 12 % and 6 %
@@ -772,7 +774,13 @@ cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const Po
         }
     }
     const bool rows_grid = ps.is_grid && ps.grid.count[1] > 1;  // the rows body can take it
-    const int64_t four_from = (rows_grid && !chunk_open) ? 131072 : 32768;
+    int64_t four_from = (rows_grid && !chunk_open) ? 131072 : 32768;
+    // small point sets against many sources: the split's S <= 8 ranks leave most SMs idle, the
+    // chunked launch spreads the sources over all of them (3,984 sources: 2,048 to 24,576
+    // scatter points ran 1.2-2.4x faster, 100^2 and 150^2 slices 1.5x and 1.2x); below about
+    // 5e6 evaluations its fixed cost outweighs that (249 sources on 101^2: 21 -> 35 us)
+    if (chunk_open && n >= 1024 && static_cast<double>(n) * static_cast<double>(ps.m) >= 5e6)
+        four_from = 2048;
     const int64_t two_from = rows_grid ? 32768 : INT64_MAX;
     if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s, scratch_ok);
     if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s, scratch_ok);
