@@ -222,6 +222,18 @@ class Engine {
     int sms = 1;
     char* d_arena = nullptr;
     char* h_arena = nullptr;
+    // the pinned arena's address for kernels (under unified addressing every cudaHostAlloc
+    // buffer is device-addressable): field kernels write results of up to kDirectOutBytes
+    // straight into a request's host block, where a copy's fixed cost would dominate; larger
+    // results (and all, when NULL) go through the device arena and the copy engine
+    char* h_arena_dev = nullptr;
+    static constexpr size_t kDirectOutBytes = 1u << 20;
+    // where a request's field kernel writes its result: its host block, or NULL for its device
+    // block
+    char* direct_out(const Request& r) const {
+        return (h_arena_dev && r.out_bytes <= kDirectOutBytes) ? h_arena_dev + r.h_off + r.h_out
+                                                               : nullptr;
+    }
     RangeAllocator dev_alloc, host_alloc;
     std::vector<Slot> slots;
     std::deque<Geometry> geoms;  // a deque: references stay valid while geometries are added
@@ -338,9 +350,11 @@ class Engine {
             PointSet ps = r.ps;
             if (!ps.is_grid) ps.pts = reinterpret_cast<const float*>(d + L.pts);
             // device memory only from the engine's budgeted arena: no partial-sum scratch
-            if ((e = launch_field(g.st, r.field, SUM_PLAIN, packed, n, ps, d + L.out, s, false)) != cudaSuccess)
+            char* direct = direct_out(r);
+            if ((e = launch_field(g.st, r.field, SUM_PLAIN, packed, n, ps, direct ? direct : d + L.out,
+                                  s, false)) != cudaSuccess)
                 return e;
-            if (r.out_bytes &&
+            if (!direct && r.out_bytes &&
                 (e = cudaMemcpyAsync(h + r.h_out, d + L.out, r.out_bytes, cudaMemcpyDeviceToHost, s)) !=
                     cudaSuccess)
                 return e;
@@ -364,10 +378,11 @@ class Engine {
             auto* packed = reinterpret_cast<PackedSource*>(d + o_pk);
             if ((e = launch_repack(g.d_packed, nullptr, nullptr, ap, n, packed, s)) != cudaSuccess)
                 return e;
-            if ((e = launch_field(g.st, FIELD_PRESSURE, SUM_PLAIN, packed, n, r.ps, d + o_out, s, false)) !=
-                cudaSuccess)
+            char* direct = direct_out(r);
+            if ((e = launch_field(g.st, FIELD_PRESSURE, SUM_PLAIN, packed, n, r.ps,
+                                  direct ? direct : d + o_out, s, false)) != cudaSuccess)
                 return e;
-            if (r.out_bytes &&
+            if (!direct && r.out_bytes &&
                 (e = cudaMemcpyAsync(h + r.h_out, d + o_out, r.out_bytes, cudaMemcpyDeviceToHost, s)) !=
                     cudaSuccess)
                 return e;
@@ -414,7 +429,8 @@ class Engine {
             J.g = r.ps.grid;
             J.pts = r.ps.is_grid ? nullptr : reinterpret_cast<const float*>(d + L.pts);
             J.m = r.ps.m;
-            J.out = d + L.out;
+            char* direct = direct_out(r);
+            J.out = direct ? direct : d + L.out;
             J.partial = r.chunks > 1 ? reinterpret_cast<float2*>(d + L.part) : nullptr;
             J.field = r.field;
             J.is_grid = r.ps.is_grid ? 1 : 0;
@@ -470,7 +486,7 @@ class Engine {
         for (size_t j = 0; j < rq.size(); ++j) {
             Request& r = *rq[j];
             const FieldLayout L = field_layout(gs[j]->n, r);
-            if (r.out_bytes &&
+            if (r.out_bytes && !direct_out(r) &&
                 (e = cudaMemcpyAsync(h_arena + r.h_off + r.h_out, d_arena + r.d_off + L.out,
                                      r.out_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
                 return e;
@@ -749,6 +765,13 @@ extern "C" int32_t AFC_ServeCreate(const AfcServeConfig* cfg, void** engine) {
     }
     e->dev_alloc = RangeAllocator(cfg->hbm_budget_bytes);
     e->host_alloc = RangeAllocator(cfg->pinned_bytes);
+    {
+        void* hd = nullptr;
+        if (cudaHostGetDevicePointer(&hd, e->h_arena, 0) == cudaSuccess && hd)
+            e->h_arena_dev = static_cast<char*>(hd);
+        else
+            (void)cudaGetLastError();
+    }
     e->sms = num_sms();
     e->group_target = 2LL * e->sms;
     for (int st = 0; st < 2; ++st) {
