@@ -457,11 +457,15 @@ constexpr int64_t kChunkMaxBytes = 256LL << 20;
 // box, the partial staging tile, the store) costs about 11 iterations, and a chunked launch
 // about 20 us more than its passes (the combine launch, the drain).
 // Its source iterations ran 2.5 % slower than the single-pass kernel's at full waves (4,194,304
-// points: 0.688 against 0.671 us).  A launch of several waves loses less to a short last wave
-// than the wave count says (the blocks of that wave share their SMs with fewer others and run
-// faster: 1,048,576 points in 7 cluster-split waves took 2 % less than modelled), so against a
-// launch of two or more waves the chunked one must model kMultiWaveMargin cheaper.  It is taken
-// only at 4 point pairs per thread, where it was calibrated.
+// points: 0.688 against 0.671 us; the 256^3 grid through the rows form: 66.2 against 64.6 ms).
+// A single pass of several waves loses less to its short last wave than the wave count says
+// (that wave's blocks share their SMs with fewer others and run faster: 4,194,304 scatter
+// points in 6.7 waves took 3.5 % less than modelled), so against it the chunked launch must
+// model kMultiWaveMargin cheaper.  The general body's cluster split gains the same way (a 96^3
+// grid on the flat numbering: split in 2.8 waves 3.9 % faster than the chunked launch the model
+// preferred by 2.7 %), the rows body's did not (128^3 in 6.7 split waves: split and chunked
+// within 1 % of their modelled times, the chunked launch 2.7 % faster), so there the margin
+// applies against the single pass only.
 constexpr double kPassSetup = 11.0;
 constexpr double kChunkFixedUs = 20.0;
 constexpr double kChunkIterationUs = 0.688;
@@ -469,9 +473,9 @@ constexpr double kChunkSlowdown = 1.025;
 constexpr double kMultiWaveMargin = 0.97;
 
 // the cost the chunked launch must beat: `cost` of a launch of `blocks` blocks on `slots`
-// resident ones, less kMultiWaveMargin when that launch runs two or more waves
-double chunk_bar(double cost, int64_t blocks, int64_t slots) {
-    return (blocks + slots - 1) / slots >= 2 ? kMultiWaveMargin * cost : cost;
+// resident ones, less kMultiWaveMargin when that launch runs two or more waves and `margin`
+double chunk_bar(double cost, int64_t blocks, int64_t slots, bool margin) {
+    return (margin && (blocks + slots - 1) / slots >= 2) ? kMultiWaveMargin * cost : cost;
 }
 
 // one pass per tile (field_direct_kernel) on `slots` resident blocks
@@ -613,13 +617,13 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         if (cudaStreamIsCapturing(s, &cst) == cudaSuccess && cst == cudaStreamCaptureStatusNone) {
             const int64_t slots1 = resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn);
             double other = direct_cost(flat_blocks, n, slots1);
-            double bar = chunk_bar(other, flat_blocks, slots1);
+            double bar = chunk_bar(other, flat_blocks, slots1, true);
             for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
                 const int64_t slots = resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(S, kDyn);
                 const double c = split_cost(flat_blocks, n, S, slots);
                 if (c < other) {
                     other = c;
-                    bar = chunk_bar(c, flat_blocks * S, slots);
+                    bar = chunk_bar(c, flat_blocks * S, slots, true);
                 }
             }
             const int64_t blocks =
@@ -683,13 +687,13 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
                     cst == cudaStreamCaptureStatusNone) {
                     const int64_t slots1 = resident_blocks<field_rows_kernel<ST, SUM, PAIRS>>(1, 0);
                     double other = direct_cost(t.blocks, n, slots1);
-                    double bar = chunk_bar(other, t.blocks, slots1);
+                    double bar = chunk_bar(other, t.blocks, slots1, true);
                     for (int64_t S = 2; S <= kMaxClusterBlocks && n / S >= kSplitMinSources; ++S) {
                         const int64_t slots = resident_blocks<field_rows_split_kernel<ST, SUM, PAIRS>>(S, 0);
                         const double c = split_cost(t.blocks, n, S, slots);
                         if (c < other) {
                             other = c;
-                            bar = chunk_bar(c, t.blocks * S, slots);
+                            bar = chunk_bar(c, t.blocks * S, slots, false);
                         }
                     }
                     const int64_t blocks = resident_blocks<field_rows_chunk_kernel<ST, PAIRS>>(1, 0);
