@@ -449,13 +449,13 @@ int64_t split_width(int64_t blocks, int64_t n, Slots slots) {
 constexpr int64_t kChunkSources = 1;
 constexpr int64_t kChunkMaxBytes = 256LL << 20;
 
-// Modelled time of the general body's launch options over `tiles` point tiles of n sources
-// each, in source iterations of one block (about 0.67 us at 4 point pairs per thread on a
-// GB300).  Calibrated on 3,984 sources and 65,536 to 4,194,304
-// scatter points: an item of 2,048 points and 210 sources took 148.5 us against 140.6 us of
-// source iterations, so the set-up of a pass over a source range (its points, their bounding
-// box, the partial staging tile, the store) costs about 11 iterations, and a chunked launch
-// about 20 us more than its passes (the combine launch, the drain).
+// Modelled time of a launch's options over `tiles` point tiles of n sources each, in source
+// iterations of one block (about 0.67 us at 4 point pairs per thread on a GB300).  Calibrated on
+// 3,984 sources and 65,536 to 4,194,304 scatter points: a pass of 2,048 points over 210 sources
+// took 148.5 us against 140.6 us of source iterations, so the set-up of a pass over a source
+// range (its points, their bounding box, the partial staging tile, the store) costs about 11
+// iterations, and a chunked launch about 20 us more than its passes (the combine launch, the
+// drain).
 // Its source iterations ran 2.5 % slower than the single-pass kernel's at full waves (4,194,304
 // points: 0.688 against 0.671 us; the 256^3 grid through the rows form: 66.2 against 64.6 ms).
 // A single pass of several waves loses less to its short last wave than the wave count says
