@@ -15,7 +15,8 @@
 //
 // Precisions
 //   split BF16: A = Ah + Al, B = Bh + Bl (hi = bf16(x), lo = bf16(x - hi)); C = Ah Bh + Ah Bl +
-//     Al Bh accumulated in FP32 (three K-segments of one accumulation), ~16 significant bits.
+//     Al Bh accumulated in FP32 (the three products interleaved in each K block of one
+//     accumulation), ~16 significant bits.
 //   FP16 row-scaled: each row of G scaled by a power of two so that its largest entry is ~1,
 //     one FP16 GEMM, the scale undone in the epilogue (exact).
 //
@@ -38,8 +39,9 @@
 // Per SM and K block this moves 32 (FP16) or 64 KB (split BF16) for 4 or 12 MMA steps of
 // 128 x 256 x 16, two thirds (FP16) or four ninths (split BF16) of the operand bytes a 128 x 256
 // single-CTA tile reads for the same work.
-// Every mbarrier wait is bounded; on time-out the CTA records an error code, lets its copies in
-// flight land (bounded) and frees its tensor memory before it returns.
+// Every mbarrier wait is bounded by a second of the global timer; on time-out the CTA records an
+// error code, lets its copies in flight land (bounded) and frees its tensor memory, together with
+// its peer, before it returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
