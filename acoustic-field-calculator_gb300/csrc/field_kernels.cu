@@ -610,7 +610,9 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
-    if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (!rows.use && scratch_ok && n >= 2 * kChunkSources) {
+    // the chunked launch numbers tiles x sources work items in 64 bits: only below 2^62 of them
+    const bool chunk_fits = n < (1LL << 31) && flat_blocks < (1LL << 31);
+    if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (!rows.use && scratch_ok && chunk_fits && n >= 2 * kChunkSources) {
         // chunked (not while the stream is being captured: the partial sums are allocated on
         // the stream) when the model puts it below the single pass and the cluster split
         cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
@@ -680,7 +682,7 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
         const RowsTiling& t = rows;
         if (t.use) {
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-            if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (scratch_ok && n >= 2 * kChunkSources) {
+            if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (scratch_ok && chunk_fits && n >= 2 * kChunkSources) {
                 // the chunked launch over the rows tiles, on the same terms as the flat one
                 cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
                 if (cudaStreamIsCapturing(s, &cst) == cudaSuccess &&
