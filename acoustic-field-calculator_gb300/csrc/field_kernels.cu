@@ -212,6 +212,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     GTable& gt = dynamic_gtab();
     load_theta_table(sm, c_dir_table);
     if constexpr (ST == SRC_T4010A1) load_gtab(gt);
+    // the combine launch may be scheduled now; it waits for this grid's completion
+    asm volatile("griddepcontrol.launch_dependents;");
     const int64_t end = cs.start(blockIdx.x + 1);
     for (int64_t it = cs.start(blockIdx.x); it < end;) {
         const int64_t tile = it / cs.chunks;
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     RowsTable& rt = rs.rt;
     load_theta_table(sm, c_dir_table);
     load_rows_table(rt);
+    asm volatile("griddepcontrol.launch_dependents;");
     const int tx = threadIdx.x & ((1 << tx_log2) - 1);
     const int ty = threadIdx.x >> tx_log2;
     const int64_t c0 = g.count[0], c1 = g.count[1];
@@ -290,6 +293,9 @@ __global__ void __launch_bounds__(256)
                                const PackedSource* __restrict__ src, int64_t n, GridDev g,
                                const float* __restrict__ pts, int64_t m, int field,
                                void* __restrict__ out) {
+    // launched as a programmatic dependent of the chunk kernel: its partial sums are complete
+    // and visible once this returns (a no-op when launched without that attribute)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < m;
          q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t t0 = tm.tile_of(q) * cs.chunks;
@@ -593,11 +599,22 @@ cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& p
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
+        // a programmatic dependent of the chunk kernel: its launch overlaps that grid's tail
         const int64_t want = (ps.m + 255) / 256, cap = 8LL * num_sms();
-        field_chunk_combine_kernel<GRID><<<static_cast<unsigned>(want < cap ? want : cap), 256, 0, s>>>(
-            static_cast<const float2*>(partial), cs, tm, src, n, ps.grid, ps.pts, ps.m, field, out);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(static_cast<unsigned>(want < cap ? want : cap));
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, field_chunk_combine_kernel<GRID>,
+                               static_cast<const float2*>(partial), cs, tm, src, n, ps.grid,
+                               ps.pts, ps.m, field, out);
         count_launch();
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     const cudaError_t ef = cudaFreeAsync(partial, s);
     return e != cudaSuccess ? e : ef;
