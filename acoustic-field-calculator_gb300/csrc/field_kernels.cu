@@ -64,6 +64,11 @@ __device__ __forceinline__ GTable& dynamic_gtab() {
     return *reinterpret_cast<GTable*>(afc_dyn_smem);
 }
 
+// The field kernels run as programmatic dependents of the launch before them on the stream (the
+// source packing, normally): they fill their tables first and wait here before they read
+// anything that launch may have written.  A no-op without a programmatic predecessor.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int ST, int SUM, bool GRID, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
     field_direct_kernel(const PackedSource* __restrict__ src, int64_t n, GridDev g,
@@ -73,6 +78,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     GTable& gt = dynamic_gtab();
     load_theta_table(sm, c_dir_table);
     if constexpr (ST == SRC_T4010A1) load_gtab(gt);
+    pdl_wait();
     const int64_t first = static_cast<int64_t>(blockIdx.x) * (kThreads * 2 * PAIRS);
     block_points<ST, SUM, PAIRS>(sm, gt, src, n, GRID, g, pts, m, first, field, out);
 }
@@ -151,6 +157,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     GTable& gt = dynamic_gtab();
     load_theta_table(sm, c_dir_table);
     if constexpr (ST == SRC_T4010A1) load_gtab(gt);
+    pdl_wait();
     const unsigned S = cg::this_cluster().num_blocks();
     const int64_t first = static_cast<int64_t>(blockIdx.x / S) * (kThreads * kPPT);
     int64_t s_lo, s_hi;
@@ -212,6 +219,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     GTable& gt = dynamic_gtab();
     load_theta_table(sm, c_dir_table);
     if constexpr (ST == SRC_T4010A1) load_gtab(gt);
+    pdl_wait();
     // the combine launch may be scheduled now; it waits for this grid's completion
     asm volatile("griddepcontrol.launch_dependents;");
     const int64_t end = cs.start(blockIdx.x + 1);
@@ -251,6 +259,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     RowsTable& rt = rs.rt;
     load_theta_table(sm, c_dir_table);
     load_rows_table(rt);
+    pdl_wait();
     asm volatile("griddepcontrol.launch_dependents;");
     const int tx = threadIdx.x & ((1 << tx_log2) - 1);
     const int ty = threadIdx.x >> tx_log2;
@@ -334,6 +343,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     RowsTable& rt = rs.rt;
     load_theta_table(sm, c_dir_table);
     load_rows_table(rt);
+    pdl_wait();
     const int64_t tile = blockIdx.x / cg::this_cluster().num_blocks();
     int64_t s_lo, s_hi;
     rank_sources(n, s_lo, s_hi);
@@ -357,12 +367,15 @@ __global__ void __launch_bounds__(kThreads, 2)
     RowsTable& rt = rs.rt;
     load_theta_table(sm, c_dir_table);
     load_rows_table(rt);
+    pdl_wait();
     block_rows<ST, SUM, PAIRS>(sm, rt, src, n, g, tx_log2, tiles0, tiles1, blockIdx.x, field, out);
 }
 
 __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
                                     const float* __restrict__ k, const float* __restrict__ atten,
                                     int64_t n, PackedSource* __restrict__ out) {
+    // the field launch after this one may start its table fills now (it waits for this grid)
+    asm volatile("griddepcontrol.launch_dependents;");
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     out[j] = pack_source(st, raw, k, atten, j);
@@ -447,6 +460,47 @@ int64_t split_width(int64_t blocks, int64_t n, Slots slots) {
         }
     }
     return best;
+}
+
+// Launches a field kernel on `grid` blocks of kThreads with `dyn` bytes of dynamic shared memory
+// on s: in clusters of `cluster` blocks when that is above one, and with `pdl` as a programmatic
+// dependent of the launch before it (the kernel fills its tables, then waits in pdl_wait).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_field_kernel(void (*kernel)(KArgs...), int64_t grid, int dyn, cudaStream_t s,
+                                unsigned cluster, bool pdl, Args... args) {
+    cudaLaunchAttribute attr[2];
+    unsigned na = 0;
+    if (cluster > 1) {
+        attr[na].id = cudaLaunchAttributeClusterDimension;
+        attr[na].val.clusterDim.x = cluster;
+        attr[na].val.clusterDim.y = 1;
+        attr[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    if (pdl) {
+        attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(grid), 1, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = static_cast<size_t>(dyn);
+    cfg.stream = s;
+    cfg.attrs = na ? attr : nullptr;
+    cfg.numAttrs = na;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Whether `s` is being captured into a graph (the chunked launch's scratch and programmatic
+// dependences stay out of captured work).
+bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cst) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return true;
+    }
+    return cst != cudaStreamCaptureStatusNone;
 }
 
 // Chunked launches (field_chunk_kernel): chunks of kChunkSources sources (one: the blocks'
@@ -568,7 +622,7 @@ constexpr int gtab_bytes() {
 // (nothing was launched).
 template <int ST, bool GRID, int PAIRS>
 cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& ps, int field,
-                           void* out, cudaStream_t s, int64_t tiles, int64_t blocks,
+                           void* out, cudaStream_t s, int64_t tiles, int64_t blocks, bool pdl,
                            const RowsTiling* rows = nullptr) {
     constexpr int kDyn = gtab_bytes<ST>();
     int64_t slots = 0;
@@ -587,16 +641,16 @@ cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& p
     if (rows) {
         tm = TileMap{rows->tx_log2, 0, rows->rows, rows->tiles0, rows->tiles1,
                      static_cast<int64_t>(ps.grid.count[0]), static_cast<int64_t>(ps.grid.count[1])};
-        field_rows_chunk_kernel<ST, PAIRS><<<grid_blocks, kThreads, 0, s>>>(
-            src, n, ps.grid, rows->tx_log2, rows->tiles0, rows->tiles1, ps.m, cs,
-            static_cast<float2*>(partial));
+        e = launch_field_kernel(field_rows_chunk_kernel<ST, PAIRS>, grid_blocks, 0, s, 1, pdl, src, n,
+                                ps.grid, rows->tx_log2, rows->tiles0, rows->tiles1, ps.m, cs,
+                                static_cast<float2*>(partial));
         count_launch();
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGetLastError();
     } else if ((e = allow_dynamic_smem<field_chunk_kernel<ST, GRID, PAIRS>>(kDyn)) == cudaSuccess) {
-        field_chunk_kernel<ST, GRID, PAIRS><<<grid_blocks, kThreads, kDyn, s>>>(
-            src, n, ps.grid, ps.pts, ps.m, cs, static_cast<float2*>(partial));
+        e = launch_field_kernel(field_chunk_kernel<ST, GRID, PAIRS>, grid_blocks, kDyn, s, 1, pdl,
+                                src, n, ps.grid, ps.pts, ps.m, cs, static_cast<float2*>(partial));
         count_launch();
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
         // a programmatic dependent of the chunk kernel: its launch overlaps that grid's tail
@@ -624,6 +678,8 @@ template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
                          void* out, cudaStream_t s, bool scratch_ok) {
     constexpr int kDyn = gtab_bytes<ST>();
+    const bool capturing = stream_capturing(s);
+    const bool pdl = !capturing;
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
     const RowsTiling rows = ps.is_grid ? rows_tiling(ps.grid, ps.m, PAIRS) : RowsTiling{};
@@ -632,8 +688,7 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (!rows.use && scratch_ok && chunk_fits && n >= 2 * kChunkSources) {
         // chunked (not while the stream is being captured: the partial sums are allocated on
         // the stream) when the model puts it below the single pass and the cluster split
-        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
-        if (cudaStreamIsCapturing(s, &cst) == cudaSuccess && cst == cudaStreamCaptureStatusNone) {
+        if (!capturing) {
             const int64_t slots1 = resident_blocks<field_direct_kernel<ST, SUM, false, PAIRS>>(1, kDyn);
             double other = direct_cost(flat_blocks, n, slots1);
             double bar = chunk_bar(other, flat_blocks, slots1, true);
@@ -650,12 +705,10 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
                            : resident_blocks<field_chunk_kernel<ST, false, PAIRS>>(1, kDyn);
             if (chunk_cost(flat_blocks, n, blocks) < bar) {
                 const cudaError_t e =
-                    ps.is_grid ? launch_chunked<ST, true, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks)
-                               : launch_chunked<ST, false, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks);
+                    ps.is_grid ? launch_chunked<ST, true, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks, pdl)
+                               : launch_chunked<ST, false, PAIRS>(src, n, ps, field, out, s, flat_blocks, blocks, pdl);
                 if (e != cudaErrorMemoryAllocation) return e;
             }
-        } else {
-            (void)cudaGetLastError();
         }
     }
     if (!rows.use) {
@@ -666,30 +719,20 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
                           : resident_blocks<field_split_kernel<ST, SUM, false, PAIRS>>(w, kDyn);
         });
         if (S >= 2 && flat_blocks * S <= 0x7fffffffLL) {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(static_cast<unsigned>(flat_blocks * S), 1, 1);
-            cfg.blockDim = dim3(kThreads, 1, 1);
-            cfg.dynamicSmemBytes = kDyn;
-            cfg.stream = s;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = static_cast<unsigned>(S);
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
+            const unsigned cl = static_cast<unsigned>(S);
             cudaError_t e;
             if (ps.is_grid) {
                 e = allow_dynamic_smem<field_split_kernel<ST, SUM, true, PAIRS>>(kDyn);
                 if (e == cudaSuccess)
-                    e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, true, PAIRS>, src, n,
-                                           ps.grid, static_cast<const float*>(nullptr), ps.m,
-                                           field, out);
+                    e = launch_field_kernel(field_split_kernel<ST, SUM, true, PAIRS>, flat_blocks * S,
+                                            kDyn, s, cl, pdl, src, n, ps.grid,
+                                            static_cast<const float*>(nullptr), ps.m, field, out);
             } else {
                 e = allow_dynamic_smem<field_split_kernel<ST, SUM, false, PAIRS>>(kDyn);
                 if (e == cudaSuccess)
-                    e = cudaLaunchKernelEx(&cfg, field_split_kernel<ST, SUM, false, PAIRS>, src, n,
-                                           ps.grid, ps.pts, ps.m, field, out);
+                    e = launch_field_kernel(field_split_kernel<ST, SUM, false, PAIRS>, flat_blocks * S,
+                                            kDyn, s, cl, pdl, src, n, ps.grid, ps.pts, ps.m, field,
+                                            out);
             }
             count_launch();
             return e != cudaSuccess ? e : cudaGetLastError();
@@ -701,9 +744,7 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
             if (t.blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
             if constexpr (PAIRS == 4 && SUM == SUM_PLAIN) if (scratch_ok && chunk_fits && n >= 2 * kChunkSources) {
                 // the chunked launch over the rows tiles, on the same terms as the flat one
-                cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
-                if (cudaStreamIsCapturing(s, &cst) == cudaSuccess &&
-                    cst == cudaStreamCaptureStatusNone) {
+                if (!capturing) {
                     const int64_t slots1 = resident_blocks<field_rows_kernel<ST, SUM, PAIRS>>(1, 0);
                     double other = direct_cost(t.blocks, n, slots1);
                     double bar = chunk_bar(other, t.blocks, slots1, true);
@@ -718,11 +759,9 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
                     const int64_t blocks = resident_blocks<field_rows_chunk_kernel<ST, PAIRS>>(1, 0);
                     if (chunk_cost(t.blocks, n, blocks) < bar) {
                         const cudaError_t e = launch_chunked<ST, true, PAIRS>(
-                            src, n, ps, field, out, s, t.blocks, blocks, &t);
+                            src, n, ps, field, out, s, t.blocks, blocks, pdl, &t);
                         if (e != cudaErrorMemoryAllocation) return e;
                     }
-                } else {
-                    (void)cudaGetLastError();
                 }
             }
             const int64_t S = split_width(t.blocks, n, [](int64_t w) {
@@ -730,28 +769,18 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
                               : resident_blocks<field_rows_split_kernel<ST, SUM, PAIRS>>(w, 0);
             });
             if (S >= 2 && t.blocks * S <= 0x7fffffffLL) {
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3(static_cast<unsigned>(t.blocks * S), 1, 1);
-                cfg.blockDim = dim3(kThreads, 1, 1);
-                cfg.dynamicSmemBytes = 0;
-                cfg.stream = s;
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = static_cast<unsigned>(S);
-                attr[0].val.clusterDim.y = 1;
-                attr[0].val.clusterDim.z = 1;
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                const cudaError_t e =
-                    cudaLaunchKernelEx(&cfg, field_rows_split_kernel<ST, SUM, PAIRS>, src, n,
-                                       ps.grid, t.tx_log2, t.tiles0, t.tiles1, field, out);
+                const cudaError_t e = launch_field_kernel(
+                    field_rows_split_kernel<ST, SUM, PAIRS>, t.blocks * S, 0, s,
+                    static_cast<unsigned>(S), pdl, src, n, ps.grid, t.tx_log2, t.tiles0, t.tiles1,
+                    field, out);
                 count_launch();
                 return e != cudaSuccess ? e : cudaGetLastError();
             }
-            field_rows_kernel<ST, SUM, PAIRS><<<static_cast<unsigned>(t.blocks), kThreads, 0, s>>>(
-                src, n, ps.grid, t.tx_log2, t.tiles0, t.tiles1, field, out);
+            const cudaError_t e = launch_field_kernel(field_rows_kernel<ST, SUM, PAIRS>, t.blocks, 0, s,
+                                                      1, pdl, src, n, ps.grid, t.tx_log2, t.tiles0,
+                                                      t.tiles1, field, out);
             count_launch();
-            return cudaGetLastError();
+            return e != cudaSuccess ? e : cudaGetLastError();
         }
     }
     const int64_t blocks = flat_blocks;
@@ -760,16 +789,16 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
     if (ps.is_grid) {
         if ((e = allow_dynamic_smem<field_direct_kernel<ST, SUM, true, PAIRS>>(kDyn)) != cudaSuccess)
             return e;
-        field_direct_kernel<ST, SUM, true, PAIRS><<<static_cast<unsigned>(blocks), kThreads, kDyn, s>>>(
-            src, n, ps.grid, nullptr, ps.m, field, out);
+        e = launch_field_kernel(field_direct_kernel<ST, SUM, true, PAIRS>, blocks, kDyn, s, 1, pdl,
+                                src, n, ps.grid, static_cast<const float*>(nullptr), ps.m, field, out);
     } else {
         if ((e = allow_dynamic_smem<field_direct_kernel<ST, SUM, false, PAIRS>>(kDyn)) != cudaSuccess)
             return e;
-        field_direct_kernel<ST, SUM, false, PAIRS><<<static_cast<unsigned>(blocks), kThreads, kDyn, s>>>(
-            src, n, ps.grid, ps.pts, ps.m, field, out);
+        e = launch_field_kernel(field_direct_kernel<ST, SUM, false, PAIRS>, blocks, kDyn, s, 1, pdl,
+                                src, n, ps.grid, ps.pts, ps.m, field, out);
     }
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // Points per thread, the cluster split or the chunked launch refilling the waves.  Scatter
