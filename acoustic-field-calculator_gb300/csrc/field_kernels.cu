@@ -674,11 +674,12 @@ cudaError_t launch_chunked(const PackedSource* src, int64_t n, const PointSet& p
     return e != cudaSuccess ? e : ef;
 }
 
+// `capturing`: s is being captured into a graph, which takes neither the chunked launch nor
+// programmatic dependences.
 template <int ST, int SUM, int PAIRS>
 cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps, int field,
-                         void* out, cudaStream_t s, bool scratch_ok) {
+                         void* out, cudaStream_t s, bool scratch_ok, bool capturing) {
     constexpr int kDyn = gtab_bytes<ST>();
-    const bool capturing = stream_capturing(s);
     const bool pdl = !capturing;
     const int64_t per_block = static_cast<int64_t>(kThreads) * 2 * PAIRS;
     const int64_t flat_blocks = (ps.m + per_block - 1) / per_block;
@@ -815,16 +816,10 @@ cudaError_t launch_pairs(const PackedSource* src, int64_t n, const PointSet& ps,
 template <int ST>
 cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const PointSet& ps,
                       int field, void* out, cudaStream_t s, bool scratch_ok) {
+    const bool capturing = stream_capturing(s);
     if (sum_mode == SUM_COMPENSATED)
-        return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s, false);
-    bool chunk_open = scratch_ok;
-    if (chunk_open) {
-        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
-        if (cudaStreamIsCapturing(s, &cst) != cudaSuccess || cst != cudaStreamCaptureStatusNone) {
-            (void)cudaGetLastError();
-            chunk_open = false;
-        }
-    }
+        return launch_pairs<ST, SUM_COMPENSATED, 2>(src, n, ps, field, out, s, false, capturing);
+    const bool chunk_open = scratch_ok && !capturing;
     const bool rows_grid = ps.is_grid && ps.grid.count[1] > 1;  // the rows body can take it
     int64_t four_from = (rows_grid && !chunk_open) ? 131072 : 32768;
     // small point sets against many sources: the split's S <= 8 ranks leave most SMs idle, the
@@ -834,9 +829,11 @@ cudaError_t launch_st(int sum_mode, const PackedSource* src, int64_t n, const Po
     if (chunk_open && n >= 1024 && static_cast<double>(n) * static_cast<double>(ps.m) >= 5e6)
         four_from = 2048;
     const int64_t two_from = rows_grid ? 32768 : INT64_MAX;
-    if (ps.m >= four_from) return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s, scratch_ok);
-    if (ps.m >= two_from) return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s, scratch_ok);
-    return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s, scratch_ok);
+    if (ps.m >= four_from)
+        return launch_pairs<ST, SUM_PLAIN, 4>(src, n, ps, field, out, s, scratch_ok, capturing);
+    if (ps.m >= two_from)
+        return launch_pairs<ST, SUM_PLAIN, 2>(src, n, ps, field, out, s, scratch_ok, capturing);
+    return launch_pairs<ST, SUM_PLAIN, 1>(src, n, ps, field, out, s, scratch_ok, capturing);
 }
 
 }  // namespace
