@@ -14,7 +14,8 @@
 //
 // Sizes are small (m <= 64 foci, n ~ 1e3 sources in the serving mix): G build is one thread per
 // pair; R is one block per entry; the iterations run in a single block so that the 100
-// dependent steps cost block barriers, not kernel launches.
+// dependent steps cost block barriers, not kernel launches (up to 64 foci with R in shared
+// memory and every row of a product summed at once).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -106,6 +107,7 @@ __global__ void column_abs_sum_kernel(const float2* __restrict__ g, int64_t n, i
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float s = 0.f;
+#pragma unroll 8
     for (int64_t i = 0; i < m; ++i) {
         const float2 v = g[i * n + j];
         s += hypotf(v.x, v.y);
@@ -181,6 +183,61 @@ __global__ void __launch_bounds__(kIterThreads)
     }
 }
 
+// The same iteration for up to kGspatSmemFoci foci, R held in shared memory and every row of a
+// product summed at once: kGspatRowThreads threads per row, thread `sub` summing columns sub,
+// sub + 16, ... in order, then the 16 partial sums added by a butterfly within the half-warp.
+// The row's first thread writes the row's new p into the other half of a double buffer, so one
+// barrier per iteration separates an iteration's reads of p from the next one's writes.
+constexpr int64_t kGspatSmemFoci = 64;
+constexpr int kGspatRowThreads = 16;
+
+__global__ void __launch_bounds__(kGspatSmemFoci * kGspatRowThreads, 1)
+    gspat_iterate_smem_kernel(const float2* __restrict__ r, const float* __restrict__ amps,
+                              int m, int repeat, float2* __restrict__ p_out) {
+    __shared__ float2 s_r[kGspatSmemFoci * kGspatSmemFoci];
+    __shared__ float2 s_p[2][kGspatSmemFoci];
+    __shared__ float s_amp[kGspatSmemFoci];
+    for (int i = threadIdx.x; i < m * m; i += blockDim.x) s_r[i] = r[i];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        s_amp[i] = amps[i];
+        s_p[0][i] = make_float2(amps[i], 0.f);
+    }
+    __syncthreads();
+    const int row = threadIdx.x / kGspatRowThreads, sub = threadIdx.x % kGspatRowThreads;
+    const bool live = row < m;  // the block is whole warps: the last half-warp may have no row
+    const float2* rr = s_r + (live ? row : 0) * m;
+    int cur = 0;
+    for (int it = 0;; ++it) {
+        const float2* p = s_p[cur];
+        float2 acc = make_float2(0.f, 0.f);
+        if (live) {
+            for (int c = sub; c < m; c += kGspatRowThreads) {
+                const float2 t = cmul(rr[c], p[c]);
+                acc.x += t.x;
+                acc.y += t.y;
+            }
+        }
+#pragma unroll
+        for (int o = kGspatRowThreads / 2; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        if (live && sub == 0) {
+            if (it == repeat) {
+                const float a = hypotf(acc.x, acc.y);
+                const float s = s_amp[row] * s_amp[row] / (a * a);
+                p_out[row] = make_float2(acc.x * s, acc.y * s);
+            } else {
+                const float s = s_amp[row] / hypotf(acc.x, acc.y);
+                s_p[cur ^ 1][row] = make_float2(acc.x * s, acc.y * s);
+            }
+        }
+        if (it == repeat) break;
+        cur ^= 1;
+        __syncthreads();
+    }
+}
+
 // q_j = scale_j * sum_i conj(G_ij) p_i; writes (|q_j|, arg q_j).  scale = inv_den2 or 1.
 __global__ void backpropagate_kernel(const float2* __restrict__ g, const float* __restrict__ scale,
                                      const float2* __restrict__ p, int64_t n, int64_t m,
@@ -188,6 +245,7 @@ __global__ void backpropagate_kernel(const float2* __restrict__ g, const float* 
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 8
     for (int64_t i = 0; i < m; ++i) {
         const float2 t = cmulc(g[i * n + j], p[i]);
         acc.x += t.x;
@@ -376,7 +434,13 @@ cudaError_t launch_solver(int kind, int st, const float* d_raw, const float* d_k
         column_abs_sum_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w.g, n, m, w.inv_den2);
         gspat_r_kernel<<<dim3(static_cast<unsigned>(m), static_cast<unsigned>(m)), 128, 0, s>>>(
             w.g, w.inv_den2, n, m, w.r);
-        gspat_iterate_kernel<<<1, kIterThreads, 0, s>>>(w.r, d_amps, m, repeat, w.p, w.gamma);
+        if (m <= kGspatSmemFoci) {
+            const unsigned threads = static_cast<unsigned>((m * kGspatRowThreads + 31) / 32 * 32);
+            gspat_iterate_smem_kernel<<<1, threads, 0, s>>>(w.r, d_amps, static_cast<int>(m),
+                                                            repeat, w.p);
+        } else {
+            gspat_iterate_kernel<<<1, kIterThreads, 0, s>>>(w.r, d_amps, m, repeat, w.p, w.gamma);
+        }
         backpropagate_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w.g, w.inv_den2, w.p, n, m, d_out);
         count_launch(4);
     } else if (kind == SOLVER_NAIVE) {
