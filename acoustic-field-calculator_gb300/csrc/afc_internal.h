@@ -118,6 +118,36 @@ inline cudaError_t stream_device(cudaStream_t s, int* dev) {
     return cudaStreamGetDevice(s, dev);
 }
 
+// Whether `s` is being captured into a graph (captured work takes neither the chunked field
+// launch's stream-ordered scratch nor programmatic dependences).  A failed query counts as a
+// capture.
+inline bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cst) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return true;
+    }
+    return cst != cudaStreamCaptureStatusNone;
+}
+
+// Launches `kernel` on s, with `pdl` as a programmatic dependent of the launch before it (the
+// kernel calls pdl_wait before touching that launch's data).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_after(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t dyn,
+                                cudaStream_t s, bool pdl, Args... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = dyn;
+    cfg.stream = s;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Record `msg` as this thread's last error (read back by AFC_GetLastError).
 void set_error_message(const char* msg);
 

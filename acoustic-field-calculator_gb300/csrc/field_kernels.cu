@@ -65,9 +65,8 @@ __device__ __forceinline__ GTable& dynamic_gtab() {
 }
 
 // The field kernels run as programmatic dependents of the launch before them on the stream (the
-// source packing, normally): they fill their tables first and wait here before they read
-// anything that launch may have written.  A no-op without a programmatic predecessor.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// source packing, normally): they fill their tables first and call pdl_wait before they read a
+// source.
 
 template <int ST, int SUM, bool GRID, int PAIRS>
 __global__ void __launch_bounds__(kThreads, 2)
@@ -220,8 +219,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     load_theta_table(sm, c_dir_table);
     if constexpr (ST == SRC_T4010A1) load_gtab(gt);
     pdl_wait();
-    // the combine launch may be scheduled now; it waits for this grid's completion
-    asm volatile("griddepcontrol.launch_dependents;");
+    pdl_release();  // the combine launch may be scheduled now; it waits for this grid's end
     const int64_t end = cs.start(blockIdx.x + 1);
     for (int64_t it = cs.start(blockIdx.x); it < end;) {
         const int64_t tile = it / cs.chunks;
@@ -260,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     load_theta_table(sm, c_dir_table);
     load_rows_table(rt);
     pdl_wait();
-    asm volatile("griddepcontrol.launch_dependents;");
+    pdl_release();
     const int tx = threadIdx.x & ((1 << tx_log2) - 1);
     const int ty = threadIdx.x >> tx_log2;
     const int64_t c0 = g.count[0], c1 = g.count[1];
@@ -303,8 +301,8 @@ __global__ void __launch_bounds__(256)
                                const float* __restrict__ pts, int64_t m, int field,
                                void* __restrict__ out) {
     // launched as a programmatic dependent of the chunk kernel: its partial sums are complete
-    // and visible once this returns (a no-op when launched without that attribute)
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // and visible once this returns
+    pdl_wait();
     for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < m;
          q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t t0 = tm.tile_of(q) * cs.chunks;
@@ -374,8 +372,9 @@ __global__ void __launch_bounds__(kThreads, 2)
 __global__ void pack_sources_kernel(int st, const float* __restrict__ raw,
                                     const float* __restrict__ k, const float* __restrict__ atten,
                                     int64_t n, PackedSource* __restrict__ out) {
-    // the field launch after this one may start its table fills now (it waits for this grid)
-    asm volatile("griddepcontrol.launch_dependents;");
+    // the launch after this one (a field kernel or the G build) may start its table fills now;
+    // it waits for this grid before it reads a source
+    pdl_release();
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     out[j] = pack_source(st, raw, k, atten, j);
@@ -490,17 +489,6 @@ cudaError_t launch_field_kernel(void (*kernel)(KArgs...), int64_t grid, int dyn,
     cfg.attrs = na ? attr : nullptr;
     cfg.numAttrs = na;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
-// Whether `s` is being captured into a graph (the chunked launch's scratch and programmatic
-// dependences stay out of captured work).
-bool stream_capturing(cudaStream_t s) {
-    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s, &cst) != cudaSuccess) {
-        (void)cudaGetLastError();
-        return true;
-    }
-    return cst != cudaStreamCaptureStatusNone;
 }
 
 // Chunked launches (field_chunk_kernel): chunks of kChunkSources sources (one: the blocks'

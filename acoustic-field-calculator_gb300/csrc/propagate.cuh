@@ -125,6 +125,16 @@ constexpr float kAcos5 = -0.0045999325811862946f;
 // rad, so the bin is at most 16, or wraps to 31 just below 0).
 constexpr int kDirTableSize = 32;
 
+// ------------------------------------------------------------------ launch ordering
+
+// Programmatic dependent launch.  A kernel launched with the programmatic stream serialisation
+// attribute may start before the launch ahead of it on its stream has ended: it calls pdl_wait
+// before it reads anything that launch writes or writes anything that launch reads (the wait
+// returns once that launch has completed and its writes are visible).  pdl_release lets the
+// launch after this one be scheduled from here on.  Both are no-ops in a plain launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // ------------------------------------------------------------------ MUFU operations
 
 __device__ __forceinline__ float mufu_rsqrt(float x) {

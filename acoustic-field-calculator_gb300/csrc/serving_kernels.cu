@@ -27,6 +27,7 @@ __global__ void repack_split_kernel(const PackedSource* __restrict__ geom,
                                     const float* __restrict__ amps,
                                     const float* __restrict__ phases, int64_t n,
                                     PackedSource* __restrict__ out) {
+    dev::pdl_release();  // the field launch after this one may fill its tables now
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     PackedSource p = geom[j];
@@ -37,6 +38,7 @@ __global__ void repack_split_kernel(const PackedSource* __restrict__ geom,
 __global__ void repack_interleaved_kernel(const PackedSource* __restrict__ geom,
                                           const float* __restrict__ amp_phase, int64_t n,
                                           PackedSource* __restrict__ out) {
+    dev::pdl_release();  // the field launch after this one may fill its tables now
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     PackedSource p = geom[j];

@@ -89,6 +89,8 @@ __global__ void build_g_kernel(const PackedSource* __restrict__ src, int64_t n,
                                const float* __restrict__ foci, int64_t m, float2* __restrict__ g) {
     __shared__ float4 s_dir[dev::kDirTableSize];
     if (threadIdx.x < dev::kDirTableSize) s_dir[threadIdx.x] = c_dir_table_s[threadIdx.x];
+    dev::pdl_wait();  // the packed sources
+    dev::pdl_release();
     __syncthreads();
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t i = blockIdx.y;
@@ -104,6 +106,8 @@ __global__ void build_g_kernel(const PackedSource* __restrict__ src, int64_t n,
 // inv_den2[j] = 1 / (sum_i |G_ij|)^2
 __global__ void column_abs_sum_kernel(const float2* __restrict__ g, int64_t n, int64_t m,
                                       float* __restrict__ inv_den2) {
+    dev::pdl_wait();
+    dev::pdl_release();
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float s = 0.f;
@@ -118,6 +122,8 @@ __global__ void column_abs_sum_kernel(const float2* __restrict__ g, int64_t n, i
 // R[i, k] = sum_j G_ij conj(G_kj) inv_den2_j, one block per entry.
 __global__ void gspat_r_kernel(const float2* __restrict__ g, const float* __restrict__ inv_den2,
                                int64_t n, int64_t m, float2* __restrict__ r) {
+    dev::pdl_wait();
+    dev::pdl_release();
     const int64_t i = blockIdx.y, k = blockIdx.x;
     const float2* gi = g + i * n;
     const float2* gk = g + k * n;
@@ -162,6 +168,8 @@ __device__ __forceinline__ void block_matvec(const float2* __restrict__ mat, con
 __global__ void __launch_bounds__(kIterThreads)
     gspat_iterate_kernel(const float2* __restrict__ r, const float* __restrict__ amps, int64_t m,
                          int repeat, float2* p, float2* gamma) {
+    dev::pdl_wait();
+    dev::pdl_release();
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) p[i] = make_float2(amps[i], 0.f);
     __syncthreads();
     for (int it = 0;; ++it) {
@@ -197,6 +205,8 @@ __global__ void __launch_bounds__(kGspatSmemFoci * kGspatRowThreads, 1)
     __shared__ float2 s_r[kGspatSmemFoci * kGspatSmemFoci];
     __shared__ float2 s_p[2][kGspatSmemFoci];
     __shared__ float s_amp[kGspatSmemFoci];
+    dev::pdl_wait();
+    dev::pdl_release();
     for (int i = threadIdx.x; i < m * m; i += blockDim.x) s_r[i] = r[i];
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
         s_amp[i] = amps[i];
@@ -242,6 +252,8 @@ __global__ void __launch_bounds__(kGspatSmemFoci * kGspatRowThreads, 1)
 __global__ void backpropagate_kernel(const float2* __restrict__ g, const float* __restrict__ scale,
                                      const float2* __restrict__ p, int64_t n, int64_t m,
                                      float* __restrict__ out) {
+    dev::pdl_wait();
+    dev::pdl_release();
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float2 acc = make_float2(0.f, 0.f);
@@ -386,12 +398,14 @@ cudaError_t launch_build_g(int st, const float* d_raw, const float* d_k, const f
     cudaError_t e = launch_pack_sources(st, d_raw, d_k, d_atten, n, packed, s);
     if (e != cudaSuccess) return e;
     const dim3 grid(blocks_for(n, 128), static_cast<unsigned>(m));
-    if (st == SRC_T4010A1)
-        build_g_kernel<SRC_T4010A1><<<grid, 128, 0, s>>>(packed, n, d_foci, m, d_g);
-    else
-        build_g_kernel<SRC_SPHERE><<<grid, 128, 0, s>>>(packed, n, d_foci, m, d_g);
+    const bool pdl = !stream_capturing(s);
+    e = st == SRC_T4010A1
+            ? launch_after(build_g_kernel<SRC_T4010A1>, grid, dim3(128), 0, s, pdl, packed, n,
+                           d_foci, m, d_g)
+            : launch_after(build_g_kernel<SRC_SPHERE>, grid, dim3(128), 0, s, pdl, packed, n,
+                           d_foci, m, d_g);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_greedy(int st, const float* d_raw, const float* d_k, const float* d_atten,
@@ -431,17 +445,30 @@ cudaError_t launch_solver(int kind, int st, const float* d_raw, const float* d_k
     cudaError_t e = launch_build_g(st, d_raw, d_k, d_atten, n, d_foci, m, w.g, w.packed, s);
     if (e != cudaSuccess) return e;
     if (kind == SOLVER_GSPAT) {
-        column_abs_sum_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w.g, n, m, w.inv_den2);
-        gspat_r_kernel<<<dim3(static_cast<unsigned>(m), static_cast<unsigned>(m)), 128, 0, s>>>(
-            w.g, w.inv_den2, n, m, w.r);
+        // each launch a programmatic dependent of the one before (the kernels wait first)
+        const bool pdl = !stream_capturing(s);
+        if ((e = launch_after(column_abs_sum_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, s, pdl,
+                              static_cast<const float2*>(w.g), n, m, w.inv_den2)) != cudaSuccess)
+            return e;
+        if ((e = launch_after(gspat_r_kernel, dim3(static_cast<unsigned>(m), static_cast<unsigned>(m)),
+                              dim3(128), 0, s, pdl, static_cast<const float2*>(w.g),
+                              static_cast<const float*>(w.inv_den2), n, m, w.r)) != cudaSuccess)
+            return e;
         if (m <= kGspatSmemFoci) {
             const unsigned threads = static_cast<unsigned>((m * kGspatRowThreads + 31) / 32 * 32);
-            gspat_iterate_smem_kernel<<<1, threads, 0, s>>>(w.r, d_amps, static_cast<int>(m),
-                                                            repeat, w.p);
+            e = launch_after(gspat_iterate_smem_kernel, dim3(1), dim3(threads), 0, s, pdl,
+                             static_cast<const float2*>(w.r), d_amps, static_cast<int>(m), repeat,
+                             w.p);
         } else {
-            gspat_iterate_kernel<<<1, kIterThreads, 0, s>>>(w.r, d_amps, m, repeat, w.p, w.gamma);
+            e = launch_after(gspat_iterate_kernel, dim3(1), dim3(kIterThreads), 0, s, pdl,
+                             static_cast<const float2*>(w.r), d_amps, m, repeat, w.p, w.gamma);
         }
-        backpropagate_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w.g, w.inv_den2, w.p, n, m, d_out);
+        if (e != cudaSuccess) return e;
+        if ((e = launch_after(backpropagate_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, s, pdl,
+                              static_cast<const float2*>(w.g),
+                              static_cast<const float*>(w.inv_den2),
+                              static_cast<const float2*>(w.p), n, m, d_out)) != cudaSuccess)
+            return e;
         count_launch(4);
     } else if (kind == SOLVER_NAIVE) {
         real_to_complex_kernel<<<blocks_for(m, 256), 256, 0, s>>>(d_amps, m, w.p);
